@@ -1,0 +1,184 @@
+/*
+ * perigrain.h -- C ABI of the GB300 (sm_103a) PeriDEM time-integration engine.
+ *
+ * This replaces the in-process boundary of the reference simulator,
+ *   template<unsigned dim> void run_timeloop(vector<ParticleN<dim>>& PArr, Timeloop TL,
+ *                                            Contact CN, RectWall<dim> Wall)
+ * (reference src/particle/timeloop.h:501-502), and the setup/config/output plumbing around it
+ * (src/read/load_hdf5.h:42-201, src/read/read_config.h:122-297, timeloop.h:881-1014).
+ *
+ * Conventions
+ *   - Plain C types only; every function returns a pg_status (PG_OK == 0). No exceptions cross
+ *     the ABI. pg_last_error() gives a message for the last failing call on this thread.
+ *   - Host arrays are in the reference's node order: grain-major (grain g owns global nodes
+ *     [grain_node_offset[g], grain_node_offset[g+1])), nodes in the order of `Pos` in all.h5,
+ *     vectors row-major (node, component) with `dim` components.
+ *   - A handle holds one or more independent simulations ("instances"); grains of one instance
+ *     are contiguous. Grains interact only with grains of the same instance. simulate2d/3d
+ *     use one instance; the batched ensemble uses hundreds.
+ *   - One handle = one CUDA stream on the current device; calls on one handle must come from
+ *     one host thread at a time.
+ */
+#ifndef PERIGRAIN_H
+#define PERIGRAIN_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum pg_status {
+  PG_OK = 0,
+  PG_EINVAL = 1,     /* bad argument or inconsistent setup */
+  PG_ENOMEM = 2,     /* device or pinned-host allocation failed */
+  PG_ECUDA = 3,      /* a CUDA runtime call failed */
+  PG_ENAN = 4,       /* a non-finite position/velocity was detected */
+  PG_ETIMEOUT = 5,   /* a bounded device-side wait gave up */
+  PG_EIO = 6,        /* file missing, unreadable or malformed */
+  PG_ECAPACITY = 7,  /* a fixed-capacity device table overflowed (see pg_last_error) */
+  PG_ERANGE = 8,     /* a node left the coordinate range the contact grid can resolve */
+  PG_ENODEV = 9      /* no CUDA device / CUDA extension unavailable */
+} pg_status;
+
+typedef enum pg_precision {
+  PG_FP64 = 0,  /* reference arithmetic: FP64 everywhere, same operation order (parity path) */
+  PG_MIXED = 1  /* FP32 bond/contact forces and accumulation; FP64 disp/vel/pos and xi_norm */
+} pg_precision;
+
+typedef struct pg_handle pg_handle;
+
+/* Setup of all grains of all instances (the content of data/hdf5/all.h5 for every instance).
+ * Reference: ParticleN<dim> (src/particle/particle2.h:29-86), Contact (src/particle/contact.h:43-112),
+ * RectWall<dim> (contact.h:114-305), loaded by load_particles/load_contact/load_wall
+ * (src/read/load_hdf5.h:42-201). */
+typedef struct pg_setup_desc {
+  uint32_t dim;          /* 2 or 3 */
+  uint32_t n_instances;  /* >= 1 */
+  uint32_t n_grains;     /* total over instances */
+  uint32_t n_nodes;      /* total over grains */
+  const uint32_t* grain_instance;    /* [n_grains] non-decreasing instance id */
+  const uint32_t* grain_node_offset; /* [n_grains+1] */
+  /* per node, reference order */
+  const double* pos;       /* [n_nodes*dim] Pos */
+  const double* vol;       /* [n_nodes]     Vol */
+  const double* disp;      /* [n_nodes*dim] */
+  const double* vel;       /* [n_nodes*dim] */
+  const double* acc;       /* [n_nodes*dim] */
+  const double* extforce;  /* [n_nodes*dim] */
+  /* bonds: CSR over global node index; row i lists the grain-local indices of i's neighbours
+   * in NbdArr order (conn2NArr, src/read/load_hdf5.h:28-38). Every bond appears in both rows. */
+  const uint64_t* bond_offset; /* [n_nodes+1] */
+  const uint32_t* bond_local;  /* [bond_offset[n_nodes]] grain-local neighbour index */
+  /* per grain node lists (grain-local indices), CSR over grains */
+  const uint32_t* bdry_offset;    /* [n_grains+1] nonlocal boundary nodes (bdry_nodes) */
+  const uint32_t* bdry_nodes;
+  const uint32_t* clamped_offset; /* [n_grains+1] clamped_nodes */
+  const uint32_t* clamped_nodes;
+  /* per grain scalars */
+  const double* delta;
+  const double* rho;
+  const double* cnot;
+  const double* snot;
+  const int32_t* movable;
+  const int32_t* breakable;
+  const int32_t* stoppable;
+  const uint8_t* break_bonds;   /* ParticleN::break_bonds (simulate2d sets 1 for all) */
+  const uint32_t* torque_axis;  /* may be NULL when torque is disabled */
+  const double* torque_val;     /* may be NULL when torque is disabled */
+  /* per instance contact parameters (pairwise/ in all.h5, after config overrides) */
+  const double* contact_radius;
+  const double* normal_stiffness;
+  const double* friction_coefficient;
+  const double* damping_ratio;
+  /* per instance wall: allow flag, geometry and side speeds in RectWall::lrtb() order:
+   * 2D [left, right, top, bottom], 3D [x_min, y_min, z_min, x_max, y_max, z_max]. */
+  const int32_t* allow_wall;  /* [n_instances] */
+  const double* wall_geom;    /* [n_instances * 2*dim] */
+  const double* wall_speed;   /* [n_instances * 2*dim] */
+} pg_setup_desc;
+
+/* Run options (Timeloop + Contact flags, src/particle/timeloop.h:62-202, contact.h:85-108). */
+typedef struct pg_config {
+  double dt;
+  int32_t enable_fracture;
+  int32_t nl_bdry_only;
+  int32_t allow_damping;
+  int32_t allow_friction;
+  int32_t self_contact;
+  int32_t enable_torque;
+  int32_t gradient_extforce;
+  uint32_t extforce_maxstep;
+  int32_t precision;       /* pg_precision */
+  int32_t record_pairs;    /* 1: keep a per-step log of (count, hash) of contact pairs */
+  uint32_t pair_log_capacity; /* steps kept in the pair log ring (default 1024 when 0) */
+  uint32_t first_step;     /* t of the first step taken (1, or resume_ind*modulo + 1) */
+  uint32_t max_contacts;   /* per-node contact candidate capacity (default 48 when 0) */
+  uint32_t block_size;     /* threads per block for node kernels (0: autotuned default) */
+} pg_config;
+
+/* ---- lifecycle ---------------------------------------------------------------------------- */
+int pg_version(void);
+int pg_device_count(int* count);
+const char* pg_status_string(int status);
+const char* pg_last_error(void);
+void pg_config_default(pg_config* cfg);
+
+/* Copy the setup to the current CUDA device and build the device layout. */
+int pg_create(const pg_setup_desc* setup, const pg_config* cfg, pg_handle** out);
+int pg_destroy(pg_handle* h);
+
+/* ---- stepping (timeloop.h:608-879: position update, force loop, velocity update, wall move) */
+int pg_step(pg_handle* h, uint32_t nsteps);
+int pg_synchronize(pg_handle* h);
+/* Index t of the next step to be taken. */
+int pg_get_step(pg_handle* h, uint64_t* next_t);
+
+/* ---- state access (host buffers, reference node order) ------------------------------------ */
+typedef enum pg_field {
+  PG_FIELD_CURRPOS = 0,  /* CurrPos after the last step's position update */
+  PG_FIELD_VEL = 1,
+  PG_FIELD_ACC = 2,
+  PG_FIELD_FORCE = 3,    /* force density of the last step (what tc_*.h5 stores as force) */
+  PG_FIELD_DISP = 4,
+  PG_FIELD_POS = 5
+} pg_field;
+/* out: [n_nodes*dim] doubles. Synchronizes the handle's stream. */
+int pg_get_field(pg_handle* h, int field, double* out);
+/* Overwrite a field (PG_FIELD_DISP/VEL/ACC/POS) -- used by resume and by the
+ * reset_partzero_y hook (timeloop.h:629-650). Writing POS keeps the bond reference vectors
+ * xi (computed from the positions given at creation) unchanged, as the reference does. */
+int pg_set_field(pg_handle* h, int field, const double* in);
+/* alive[b] = 1 if bond b (CSR order given at creation) is intact. */
+int pg_get_bond_alive(pg_handle* h, uint8_t* alive);
+/* Step at which each bond broke (0 = intact), CSR order. */
+int pg_get_bond_break_step(pg_handle* h, uint32_t* step);
+/* Replace the alive set (resume with enable_fracture: Connectivity reloaded, timeloop.h:530-536). */
+int pg_set_bond_alive(pg_handle* h, const uint8_t* alive);
+/* Wall reactions of the last step: [n_instances * 2*dim * dim], RectWall::get_reaction() order. */
+int pg_get_reaction(pg_handle* h, double* out);
+/* Current wall geometry [n_instances * 2*dim] (lrtb order) and override it. */
+int pg_get_wall(pg_handle* h, double* out);
+int pg_set_wall(pg_handle* h, const double* geom);
+/* Grain flags (set_movable_index / set_stoppable_index hooks, timeloop.h:612-627). */
+int pg_set_grain_flags(pg_handle* h, uint32_t grain, int32_t movable, int32_t stoppable);
+
+/* ---- diagnostics ---------------------------------------------------------------------------- */
+/* Per-step contact-pair log (needs cfg.record_pairs): for the last `n` steps ending at the
+ * last completed step, count[k] = number of node pairs that passed the contact test
+ * (|x_q - x_p| <= R_c') and hash[k] = wrapping sum of splitmix64((gid_p << 32) | gid_q). */
+int pg_get_pair_log(pg_handle* h, uint32_t n, uint64_t* count, uint64_t* hash);
+/* Sticky device error word (PG_ECAPACITY/PG_ERANGE/...), 0 if none; also "nodes too close"
+ * events (dir_norm == 0 in contact.h:737) counted since creation. */
+int pg_get_device_status(pg_handle* h, int32_t* status, uint64_t* too_close_events);
+/* Number of kernel launches issued by the last pg_step call. */
+int pg_get_launch_count(pg_handle* h, uint64_t* launches);
+/* Per-kernel device time of the last pg_step call (CUDA events; needs timing enabled). */
+int pg_set_timing(pg_handle* h, int32_t enable);
+int pg_get_kernel_times(pg_handle* h, double* force_ms, double* total_ms, uint64_t* force_launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PERIGRAIN_H */

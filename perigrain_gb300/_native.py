@@ -1,0 +1,156 @@
+"""ctypes bindings of the C ABI (include/perigrain.h, include/perigrain_io.h).
+
+The library is the in-tree ``libperigrain.so`` built by ``perigrain_gb300.build``. There is no
+fallback: if the library is missing or cannot be loaded, every entry point raises.
+"""
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libperigrain.so")
+
+PG_OK, PG_EINVAL, PG_ENOMEM, PG_ECUDA, PG_ENAN, PG_ETIMEOUT, PG_EIO, PG_ECAPACITY, PG_ERANGE, PG_ENODEV = range(10)
+PG_FP64, PG_MIXED = 0, 1
+FIELD = {"CurrPos": 0, "vel": 1, "acc": 2, "force": 3, "disp": 4, "pos": 5}
+
+u32p = C.POINTER(C.c_uint32)
+u64p = C.POINTER(C.c_uint64)
+i32p = C.POINTER(C.c_int32)
+f64p = C.POINTER(C.c_double)
+u8p = C.POINTER(C.c_uint8)
+
+
+class SetupDesc(C.Structure):
+    _fields_ = [
+        ("dim", C.c_uint32), ("n_instances", C.c_uint32), ("n_grains", C.c_uint32), ("n_nodes", C.c_uint32),
+        ("grain_instance", u32p), ("grain_node_offset", u32p),
+        ("pos", f64p), ("vol", f64p), ("disp", f64p), ("vel", f64p), ("acc", f64p), ("extforce", f64p),
+        ("bond_offset", u64p), ("bond_local", u32p),
+        ("bdry_offset", u32p), ("bdry_nodes", u32p), ("clamped_offset", u32p), ("clamped_nodes", u32p),
+        ("delta", f64p), ("rho", f64p), ("cnot", f64p), ("snot", f64p),
+        ("movable", i32p), ("breakable", i32p), ("stoppable", i32p), ("break_bonds", u8p),
+        ("torque_axis", u32p), ("torque_val", f64p),
+        ("contact_radius", f64p), ("normal_stiffness", f64p), ("friction_coefficient", f64p),
+        ("damping_ratio", f64p),
+        ("allow_wall", i32p), ("wall_geom", f64p), ("wall_speed", f64p),
+    ]
+
+
+class Config(C.Structure):
+    _fields_ = [
+        ("dt", C.c_double), ("enable_fracture", C.c_int32), ("nl_bdry_only", C.c_int32),
+        ("allow_damping", C.c_int32), ("allow_friction", C.c_int32), ("self_contact", C.c_int32),
+        ("enable_torque", C.c_int32), ("gradient_extforce", C.c_int32), ("extforce_maxstep", C.c_uint32),
+        ("precision", C.c_int32), ("record_pairs", C.c_int32), ("pair_log_capacity", C.c_uint32),
+        ("first_step", C.c_uint32), ("max_contacts", C.c_uint32), ("block_size", C.c_uint32),
+    ]
+
+
+CONF_FIELDS = [
+    ("timesteps", C.c_uint32), ("modulo", C.c_uint32), ("dt", C.c_double),
+    ("is_parallel", C.c_int32), ("do_resume", C.c_int32), ("wall_resume", C.c_int32),
+    ("resume_ind", C.c_uint32), ("save_file", C.c_int32), ("enable_fracture", C.c_int32),
+    ("nl_bdry_only", C.c_int32), ("allow_damping", C.c_int32), ("allow_friction", C.c_int32),
+    ("normal_stiffness", C.c_double), ("damping_ratio", C.c_double), ("friction_coefficient", C.c_double),
+    ("self_contact", C.c_int32), ("self_contact_rad", C.c_double), ("enable_torque", C.c_int32),
+    ("set_movable_index", C.c_int32), ("set_movable_timestep", C.c_int32),
+    ("set_stoppable_index", C.c_int32), ("set_stoppable_timestep", C.c_int32),
+    ("reset_partzero_y", C.c_int32), ("reset_partzero_y_timestep", C.c_uint32), ("wheel_rad", C.c_double),
+    ("wall_left", C.c_double), ("wall_right", C.c_double), ("wall_top", C.c_double), ("wall_bottom", C.c_double),
+    ("wall_x_min", C.c_double), ("wall_y_min", C.c_double), ("wall_z_min", C.c_double),
+    ("wall_x_max", C.c_double), ("wall_y_max", C.c_double), ("wall_z_max", C.c_double),
+    ("speed_wall_left", C.c_double), ("speed_wall_right", C.c_double), ("speed_wall_top", C.c_double),
+    ("speed_wall_bottom", C.c_double),
+    ("speed_wall_x_min", C.c_double), ("speed_wall_y_min", C.c_double), ("speed_wall_z_min", C.c_double),
+    ("speed_wall_x_max", C.c_double), ("speed_wall_y_max", C.c_double), ("speed_wall_z_max", C.c_double),
+    ("gradient_extforce", C.c_int32), ("extforce_maxstep", C.c_uint32),
+]
+
+
+class Conf(C.Structure):
+    _fields_ = CONF_FIELDS
+
+
+# (name, restype, argtypes) of every exported function; tests check that each is exported.
+PROTOTYPES = [
+    ("pg_version", C.c_int, []),
+    ("pg_device_count", C.c_int, [i32p]),
+    ("pg_status_string", C.c_char_p, [C.c_int]),
+    ("pg_last_error", C.c_char_p, []),
+    ("pg_config_default", None, [C.POINTER(Config)]),
+    ("pg_create", C.c_int, [C.POINTER(SetupDesc), C.POINTER(Config), C.POINTER(C.c_void_p)]),
+    ("pg_destroy", C.c_int, [C.c_void_p]),
+    ("pg_step", C.c_int, [C.c_void_p, C.c_uint32]),
+    ("pg_synchronize", C.c_int, [C.c_void_p]),
+    ("pg_get_step", C.c_int, [C.c_void_p, u64p]),
+    ("pg_get_field", C.c_int, [C.c_void_p, C.c_int, f64p]),
+    ("pg_set_field", C.c_int, [C.c_void_p, C.c_int, f64p]),
+    ("pg_get_bond_alive", C.c_int, [C.c_void_p, u8p]),
+    ("pg_get_bond_break_step", C.c_int, [C.c_void_p, u32p]),
+    ("pg_set_bond_alive", C.c_int, [C.c_void_p, u8p]),
+    ("pg_get_reaction", C.c_int, [C.c_void_p, f64p]),
+    ("pg_get_wall", C.c_int, [C.c_void_p, f64p]),
+    ("pg_set_wall", C.c_int, [C.c_void_p, f64p]),
+    ("pg_set_grain_flags", C.c_int, [C.c_void_p, C.c_uint32, C.c_int32, C.c_int32]),
+    ("pg_get_pair_log", C.c_int, [C.c_void_p, C.c_uint32, u64p, u64p]),
+    ("pg_get_device_status", C.c_int, [C.c_void_p, i32p, u64p]),
+    ("pg_get_launch_count", C.c_int, [C.c_void_p, u64p]),
+    ("pg_set_timing", C.c_int, [C.c_void_p, C.c_int32]),
+    ("pg_get_kernel_times", C.c_int, [C.c_void_p, f64p, f64p, u64p]),
+    # perigrain_io.h
+    ("pg_conf_default", None, [C.POINTER(Conf)]),
+    ("pg_conf_read_file", C.c_int, [C.POINTER(Conf), C.c_char_p]),
+    ("pg_conf_read_string", C.c_int, [C.POINTER(Conf), C.c_char_p, C.c_int]),
+    ("pg_setup_load", C.c_int, [C.c_char_p, C.c_uint32, C.c_int32, C.POINTER(C.c_void_p)]),
+    ("pg_setup_from_desc", C.c_int, [C.POINTER(SetupDesc), C.POINTER(C.c_void_p)]),
+    ("pg_setup_free", C.c_int, [C.c_void_p]),
+    ("pg_setup_desc_get", C.c_int, [C.c_void_p, C.POINTER(SetupDesc)]),
+    ("pg_setup_apply_conf", C.c_int, [C.c_void_p, C.POINTER(Conf)]),
+    ("pg_setup_save", C.c_int, [C.c_void_p, C.c_char_p]),
+    ("pg_setup_set_connectivity", C.c_int, [C.c_void_p, C.c_uint32, u32p, C.c_uint64]),
+    ("pg_write_snapshot", C.c_int, [C.c_void_p, C.c_void_p, C.c_char_p, C.c_uint32]),
+    ("pg_run_simulation", C.c_int, [C.c_char_p, C.c_uint32, C.c_int32]),
+    ("pg_h5w_new", C.c_void_p, []),
+    ("pg_h5w_add", C.c_int, [C.c_void_p, C.c_char_p, C.c_int32, C.c_uint32, u64p, C.c_void_p]),
+    ("pg_h5w_group", C.c_int, [C.c_void_p, C.c_char_p]),
+    ("pg_h5w_write", C.c_int, [C.c_void_p, C.c_char_p]),
+    ("pg_h5w_free", None, [C.c_void_p]),
+    ("pg_h5_info", C.c_int, [C.c_char_p, C.c_char_p, u32p, u64p, i32p, u32p, i32p]),
+    ("pg_h5_read", C.c_int, [C.c_char_p, C.c_char_p, C.c_int32, C.c_void_p, C.c_uint64]),
+    ("pg_h5_list", C.c_int, [C.c_char_p, C.c_char_p, C.c_char_p, C.c_uint64]),
+]
+
+_lib = None
+
+
+class PerigrainError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("perigrain status %d: %s" % (code, msg))
+        self.code = code
+
+
+def lib():
+    """Load libperigrain.so (raises if it is missing -- there is no CPU fallback)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError("perigrain_gb300 native library not built: %s (run perigrain_gb300.build.build())"
+                              % LIB_PATH)
+        L = C.CDLL(LIB_PATH)
+        for name, res, args in PROTOTYPES:
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(rc):
+    if rc != PG_OK:
+        msg = lib().pg_last_error()
+        raise PerigrainError(rc, msg.decode() if msg else "")
+    return rc
+
+
+def ptr(a, ctype):
+    return a.ctypes.data_as(C.POINTER(ctype))

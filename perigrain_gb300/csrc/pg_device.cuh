@@ -1,0 +1,166 @@
+// Device-side data layout and helpers of the GB300 PeriDEM engine.
+//
+// Layout in HBM (one handle, all instances):
+//   * node vectors are stored AoS with a stride of S doubles per node, S = 2 (2D, one
+//     double2 load) or 4 (3D, padded: two double2 loads);
+//   * bonds use a warp-sliced ELL layout ("SELL-32"): the 32 nodes of warp chunk c own
+//     chunk_deg[c] * 32 slots starting at chunk_slot[c]; bond k of node (32c + lane) sits in
+//     slot chunk_slot[c] + 32k + lane, so the k-th bond of a whole warp is one coalesced
+//     128-byte (col) / 256-byte (xi_norm) access. Row order within a node is the reference's
+//     NbdArr order; padding slots are never alive;
+//   * the alive set is one 32-bit word per (chunk, k): bit `lane` is bond k of that lane, so a
+//     warp reads its alive bits with one broadcast load and writes them back with one ballot;
+//   * the contact grid is a per-instance hashed uniform grid (cell >= R_c) rebuilt every step by
+//     a counting sort of the nodes by bucket (one radix digit that spans the whole bucket range),
+//     whose exclusive scan doubles as the cell-start table.
+#pragma once
+#include <cstdint>
+
+#include "../../include/perigrain.h"
+
+namespace pg {
+
+constexpr uint32_t NONE = 0xffffffffu;
+constexpr int MAX_CAND = 64;        // hard cap of contact candidates held per node
+constexpr int FINAL_THREADS = 1024; // threads of the per-step finalize kernel
+constexpr int WREC_SMEM_CAP = 16384;// wall-reaction records sorted in shared memory per step
+
+enum GrainFlag : uint32_t {
+  GF_MOVABLE = 1u,
+  GF_BREAKABLE = 2u,
+  GF_STOPPABLE = 4u,
+  GF_BREAK_BONDS = 8u,
+};
+
+struct GrainDev {
+  uint32_t node_begin, node_end;
+  uint32_t inst;
+  uint32_t flags;
+  double rho, one_over_rho, cnot, snot;
+  double torque_val;
+  uint32_t torque_axis;
+  uint32_t pad;
+};
+
+struct InstDev {
+  double contact_rad, normal_stiffness, friction_coefficient, damping_ratio;
+  double origin[3];
+  double cell;          // grid cell edge (>= contact_rad)
+  float inv_cell_f;     // 1/cell in float (cell coordinates are computed in FP32)
+  float cell_f;
+  float range_f;        // |x - origin| beyond this cannot be resolved in FP32 -> PG_ERANGE
+  uint32_t table_off, table_mask;
+  uint32_t node_begin, node_end;
+  int32_t allow_wall;
+  double wall[6];
+  double wall_speed[6];
+};
+
+// A wall interaction of one node with one wall side, kept so that the reaction sums can be
+// replayed in the reference's serial node order (contact.h:339, :374, :411-412, :428).
+struct WallRec {
+  double a_normal;   // vol * c_sign * F            (subtracted from reaction[dir])
+  double a_t1;       // vol * friction (tangent 1)  (subtracted from reaction[t1])
+  double a_t2;       // vol * friction (tangent 2, 3D)
+  double a_damp;     // vol * damping force         (subtracted from reaction[dir])
+  uint32_t gid;
+  uint16_t side;     // lrtb index
+  uint8_t has_fric;
+  uint8_t has_damp;
+};
+
+struct Dev {
+  uint32_t dim, N, G, I;
+  uint32_t n_chunks;
+  uint32_t table_total;
+  // node arrays
+  double *xpos, *pos, *disp, *cur, *vel_in, *vel_out, *acc, *force, *extf, *vol;
+  float* curf;  // float copy of (cur - origin) for the grid, stride SF
+  uint32_t *node_grain, *bdry_rank;
+  uint8_t *clamped, *clamp_pending;
+  // grid
+  uint32_t *cell_key, *cell_rank, *cell_count, *cell_start, *sorted;
+  uint32_t *scan_tile_sum;
+  uint32_t *scan_done;
+  // bonds (SELL-32)
+  uint32_t *chunk_slot, *chunk_deg, *chunk_word, *node_deg;
+  uint32_t* bcol;
+  double* bxin;
+  uint32_t* alive;
+  uint32_t* break_step;
+  // grains / instances
+  GrainDev* grain;
+  unsigned long long* bbox;  // [G][2*dim] ordered keys: min..., max...
+  double* torque_c;          // [G][3] centroid for torque
+  InstDev* inst;
+  double* reaction;          // [I][2*dim][dim]
+  WallRec* wrec;
+  uint32_t* wrec_count;
+  uint32_t wrec_cap;
+  // pair log
+  unsigned long long* pair_acc;  // [2]: count, hash
+  unsigned long long *log_count, *log_hash;
+  uint32_t log_cap;
+  // control
+  uint32_t* step;  // t of the step in flight
+  int32_t* status;
+  unsigned long long* too_close;
+  // config
+  double dt, hdt2, half_dt;
+  int32_t enable_fracture, nl_bdry_only, allow_damping, allow_friction, self_contact;
+  int32_t enable_torque, gradient_extforce, record_pairs;
+  uint32_t extforce_maxstep;
+  uint32_t max_cand;
+};
+
+__host__ __device__ inline unsigned long long dbl_to_ordered(double x) {
+  unsigned long long b;
+#ifdef __CUDA_ARCH__
+  b = (unsigned long long)__double_as_longlong(x);
+#else
+  __builtin_memcpy(&b, &x, 8);
+#endif
+  return (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
+}
+__host__ __device__ inline double ordered_to_dbl(unsigned long long k) {
+  unsigned long long b = (k & 0x8000000000000000ull) ? (k & 0x7fffffffffffffffull) : ~k;
+  double x;
+#ifdef __CUDA_ARCH__
+  x = __longlong_as_double((long long)b);
+#else
+  __builtin_memcpy(&x, &b, 8);
+#endif
+  return x;
+}
+
+__host__ __device__ inline uint64_t splitmix64(uint64_t x) {
+  x += 0x9e3779b97f4a7c15ull;
+  x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ull;
+  x = (x ^ (x >> 27)) * 0x94d049bb133111ebull;
+  return x ^ (x >> 31);
+}
+
+__host__ __device__ inline uint32_t morton2(uint32_t x, uint32_t y) {
+  auto spread = [](uint32_t v) {
+    v &= 0xffffu;
+    v = (v | (v << 8)) & 0x00ff00ffu;
+    v = (v | (v << 4)) & 0x0f0f0f0fu;
+    v = (v | (v << 2)) & 0x33333333u;
+    v = (v | (v << 1)) & 0x55555555u;
+    return v;
+  };
+  return spread(x) | (spread(y) << 1);
+}
+__host__ __device__ inline uint32_t morton3(uint32_t x, uint32_t y, uint32_t z) {
+  auto spread = [](uint32_t v) {
+    v &= 0x3ffu;
+    v = (v | (v << 16)) & 0x030000ffu;
+    v = (v | (v << 8)) & 0x0300f00fu;
+    v = (v | (v << 4)) & 0x030c30c3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
+  };
+  return spread(x) | (spread(y) << 1) | (spread(z) << 2);
+}
+
+}  // namespace pg

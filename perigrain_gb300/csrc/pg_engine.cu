@@ -1,0 +1,796 @@
+// Host side of the GB300 PeriDEM engine: builds the device layout from a pg_setup_desc,
+// drives the per-step kernels (captured into CUDA graphs) and implements the C ABI of
+// include/perigrain.h.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "pg_device.cuh"
+#include "pg_kernels.h"
+
+using namespace pg;
+
+static thread_local std::string g_err;
+
+static int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+#define CU(call)                                                                       \
+  do {                                                                                 \
+    cudaError_t _e = (call);                                                           \
+    if (_e != cudaSuccess)                                                             \
+      return fail(_e == cudaErrorMemoryAllocation ? PG_ENOMEM : PG_ECUDA,              \
+                  std::string(#call) + ": " + cudaGetErrorString(_e));                 \
+  } while (0)
+
+struct pg_handle {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  Dev P{};          // device pointers + config; vel_in/vel_out are set per launch
+  LaunchCfg L;
+  uint32_t dim = 2, S = 2;
+  int precision = PG_FP64;
+  uint64_t next_t = 1;
+  int vel_parity = 0;  // 0: current velocity in vel_a
+  double* vel_a = nullptr;
+  double* vel_b = nullptr;
+  bool xpos_separate = false;
+  std::vector<void*> allocs;
+  // host copies needed for mapping
+  std::vector<uint64_t> bond_offset;  // reference CSR
+  std::vector<uint32_t> grain_node_offset;
+  std::vector<uint32_t> node_deg;
+  std::vector<uint32_t> chunk_slot, chunk_word;
+  std::vector<InstDev> inst_host;
+  // graphs: one per velocity parity, each GRAPH_STEPS steps
+  static const int GRAPH_STEPS = 8;
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  uint64_t graph_launches_per = 0;
+  uint64_t last_launches = 0;
+  // timing
+  bool timing = false;
+  std::vector<cudaEvent_t> ev;
+  double force_ms = 0, total_ms = 0;
+  uint64_t force_launches = 0;
+  cudaEvent_t ev_t0 = nullptr, ev_t1 = nullptr;
+
+  ~pg_handle() {
+    if (stream) cudaStreamSynchronize(stream);
+    for (int i = 0; i < 2; ++i)
+      if (graph[i]) cudaGraphExecDestroy(graph[i]);
+    for (auto e : ev) cudaEventDestroy(e);
+    if (ev_t0) cudaEventDestroy(ev_t0);
+    if (ev_t1) cudaEventDestroy(ev_t1);
+    for (void* p : allocs) cudaFree(p);
+    if (xpos_separate) cudaFree(P.xpos);
+    if (stream) cudaStreamDestroy(stream);
+  }
+
+  template <class T>
+  cudaError_t dalloc(T** p, size_t count) {
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
+    if (e == cudaSuccess) allocs.push_back((void*)*p);
+    return e;
+  }
+};
+
+static void set_vel(pg_handle* h, Dev& P, int parity) {
+  P.vel_in = parity == 0 ? h->vel_a : h->vel_b;
+  P.vel_out = parity == 0 ? h->vel_b : h->vel_a;
+}
+
+static void enqueue_step(pg_handle* h, int parity, uint64_t* launches) {
+  Dev P = h->P;
+  set_vel(h, P, parity);
+  launch_step(P, h->L, h->stream, launches);
+}
+
+static int build_graphs(pg_handle* h) {
+  for (int par = 0; par < 2; ++par) {
+    if (h->graph[par]) {
+      cudaGraphExecDestroy(h->graph[par]);
+      h->graph[par] = nullptr;
+    }
+    cudaGraph_t g = nullptr;
+    CU(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    uint64_t n = 0;
+    int p = par;
+    for (int k = 0; k < pg_handle::GRAPH_STEPS; ++k) {
+      enqueue_step(h, p, &n);
+      p ^= 1;
+    }
+    CU(cudaStreamEndCapture(h->stream, &g));
+    cudaError_t e = cudaGraphInstantiate(&h->graph[par], g, 0);
+    cudaGraphDestroy(g);
+    CU(e);
+    h->graph_launches_per = n;
+  }
+  return PG_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
+extern "C" {
+
+int pg_version(void) { return 1; }
+
+const char* pg_last_error(void) { return g_err.c_str(); }
+
+const char* pg_status_string(int s) {
+  switch (s) {
+    case PG_OK: return "ok";
+    case PG_EINVAL: return "invalid argument";
+    case PG_ENOMEM: return "out of memory";
+    case PG_ECUDA: return "CUDA error";
+    case PG_ENAN: return "non-finite state";
+    case PG_ETIMEOUT: return "device wait timed out";
+    case PG_EIO: return "I/O error";
+    case PG_ECAPACITY: return "device table capacity exceeded";
+    case PG_ERANGE: return "node outside the resolvable coordinate range";
+    case PG_ENODEV: return "no CUDA device";
+  }
+  return "unknown status";
+}
+
+int pg_device_count(int* count) {
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess) {
+    *count = 0;
+    return fail(PG_ENODEV, cudaGetErrorString(e));
+  }
+  *count = n;
+  return PG_OK;
+}
+
+void pg_config_default(pg_config* c) {
+  std::memset(c, 0, sizeof(*c));
+  c->dt = 0.02 / 1e5;
+  c->allow_damping = 1;
+  c->allow_friction = 1;
+  c->self_contact = 1;
+  c->precision = PG_FP64;
+  c->pair_log_capacity = 1024;
+  c->first_step = 1;
+  c->max_contacts = 48;
+}
+
+static int validate(const pg_setup_desc* s, const pg_config* c) {
+  if (!s || !c) return fail(PG_EINVAL, "null setup or config");
+  if (s->dim != 2 && s->dim != 3) return fail(PG_EINVAL, "dim must be 2 or 3");
+  if (s->n_instances == 0 || s->n_grains == 0 || s->n_nodes == 0)
+    return fail(PG_EINVAL, "empty setup");
+  if (!s->grain_instance || !s->grain_node_offset || !s->pos || !s->vol || !s->disp || !s->vel ||
+      !s->acc || !s->extforce || !s->bond_offset || !s->bdry_offset || !s->clamped_offset ||
+      !s->delta || !s->rho || !s->cnot || !s->snot || !s->movable || !s->breakable ||
+      !s->stoppable || !s->break_bonds || !s->contact_radius || !s->normal_stiffness ||
+      !s->friction_coefficient || !s->damping_ratio || !s->allow_wall || !s->wall_geom ||
+      !s->wall_speed)
+    return fail(PG_EINVAL, "missing setup array");
+  if (s->grain_node_offset[0] != 0 || s->grain_node_offset[s->n_grains] != s->n_nodes)
+    return fail(PG_EINVAL, "grain_node_offset must start at 0 and end at n_nodes");
+  for (uint32_t g = 0; g < s->n_grains; ++g) {
+    if (s->grain_node_offset[g + 1] <= s->grain_node_offset[g])
+      return fail(PG_EINVAL, "grain " + std::to_string(g) + " has no nodes");
+    if (s->grain_instance[g] >= s->n_instances || (g && s->grain_instance[g] < s->grain_instance[g - 1]))
+      return fail(PG_EINVAL, "grain_instance must be non-decreasing and < n_instances");
+    if (c->enable_torque && s->dim == 2 && s->torque_axis && s->torque_axis[g] != 2)
+      return fail(PG_EINVAL, "2D torque requires torque_axis = 2");
+    if (c->enable_torque && (!s->torque_axis || !s->torque_val))
+      return fail(PG_EINVAL, "enable_torque needs torque_axis and torque_val");
+    if (c->enable_torque && s->torque_axis[g] > 2) return fail(PG_EINVAL, "torque_axis must be 0..2");
+  }
+  if (s->bond_offset[0] != 0) return fail(PG_EINVAL, "bond_offset[0] must be 0");
+  if (s->bond_offset[s->n_nodes] >= (1ull << 31)) return fail(PG_EINVAL, "too many bonds");
+  if (s->bond_offset[s->n_nodes] && !s->bond_local) return fail(PG_EINVAL, "missing bond_local");
+  for (uint32_t g = 0; g < s->n_grains; ++g) {
+    uint32_t n0 = s->grain_node_offset[g], n1 = s->grain_node_offset[g + 1];
+    for (uint32_t i = n0; i < n1; ++i) {
+      if (s->bond_offset[i + 1] < s->bond_offset[i]) return fail(PG_EINVAL, "bond_offset decreasing");
+      for (uint64_t b = s->bond_offset[i]; b < s->bond_offset[i + 1]; ++b)
+        if (s->bond_local[b] >= n1 - n0)
+          return fail(PG_EINVAL, "bond of node " + std::to_string(i) + " points outside its grain");
+    }
+    for (uint32_t k = s->bdry_offset[g]; k < s->bdry_offset[g + 1]; ++k)
+      if (s->bdry_nodes[k] >= n1 - n0) return fail(PG_EINVAL, "bdry node out of range");
+    for (uint32_t k = s->clamped_offset[g]; k < s->clamped_offset[g + 1]; ++k)
+      if (s->clamped_nodes[k] >= n1 - n0) return fail(PG_EINVAL, "clamped node out of range");
+  }
+  if (!(c->dt > 0)) return fail(PG_EINVAL, "dt must be positive");
+  if (c->precision != PG_FP64) return fail(PG_EINVAL, "only PG_FP64 is available in this build");
+  return PG_OK;
+}
+
+static uint32_t next_pow2(uint64_t x) {
+  uint32_t p = 1;
+  while (p < x) p <<= 1;
+  return p;
+}
+
+int pg_create(const pg_setup_desc* s, const pg_config* cfg_in, pg_handle** out) {
+  if (!out) return fail(PG_EINVAL, "null out");
+  *out = nullptr;
+  pg_config cfg = *cfg_in;
+  int rc = validate(s, &cfg);
+  if (rc) return rc;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(PG_ENODEV, "no CUDA device");
+  if (cfg.pair_log_capacity == 0) cfg.pair_log_capacity = 1024;
+  if (cfg.max_contacts == 0) cfg.max_contacts = 48;
+  if (cfg.max_contacts > (uint32_t)MAX_CAND) cfg.max_contacts = MAX_CAND;
+  if (cfg.first_step == 0) cfg.first_step = 1;
+
+  CU(kernels_init());
+
+  std::unique_ptr<pg_handle> h(new pg_handle);
+  CU(cudaGetDevice(&h->device));
+  CU(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+  const uint32_t D = s->dim, S = (D == 2) ? 2 : 4, N = s->n_nodes, G = s->n_grains, I = s->n_instances;
+  h->dim = D;
+  h->S = S;
+  h->precision = cfg.precision;
+  h->next_t = cfg.first_step;
+  if (cfg.block_size) h->L.force_block = std::max(32u, (cfg.block_size / 32) * 32);
+  Dev& P = h->P;
+  P.dim = D;
+  P.N = N;
+  P.G = G;
+  P.I = I;
+  P.n_chunks = (N + 31) / 32;
+  P.dt = cfg.dt;
+  P.hdt2 = (cfg.dt * cfg.dt) * 0.5;
+  P.half_dt = 0.5 * cfg.dt;
+  P.enable_fracture = cfg.enable_fracture;
+  P.nl_bdry_only = cfg.nl_bdry_only;
+  P.allow_damping = cfg.allow_damping;
+  P.allow_friction = cfg.allow_friction;
+  P.self_contact = cfg.self_contact;
+  P.enable_torque = cfg.enable_torque;
+  P.gradient_extforce = cfg.gradient_extforce;
+  P.record_pairs = cfg.record_pairs;
+  P.extforce_maxstep = cfg.extforce_maxstep;
+  P.max_cand = cfg.max_contacts;
+
+  h->grain_node_offset.assign(s->grain_node_offset, s->grain_node_offset + G + 1);
+  h->bond_offset.assign(s->bond_offset, s->bond_offset + N + 1);
+
+  // ---- node arrays (reference order; stride S) ----
+  std::vector<double> tmp((size_t)N * S, 0.0);
+  auto pack = [&](const double* src) {
+    std::fill(tmp.begin(), tmp.end(), 0.0);
+    for (uint32_t i = 0; i < N; ++i)
+      for (uint32_t c = 0; c < D; ++c) tmp[(size_t)i * S + c] = src[(size_t)i * D + c];
+  };
+  double** vecs[] = {&P.pos, &P.disp, &P.cur, &h->vel_a, &h->vel_b, &P.acc, &P.force, &P.extf};
+  for (double** v : vecs) CU(h->dalloc(v, (size_t)N * S));
+  P.xpos = P.pos;
+  CU(h->dalloc(&P.vol, N));
+  CU(h->dalloc(&P.curf, (size_t)N * S));
+  pack(s->pos);
+  CU(cudaMemcpy(P.pos, tmp.data(), tmp.size() * 8, cudaMemcpyHostToDevice));
+  pack(s->disp);
+  CU(cudaMemcpy(P.disp, tmp.data(), tmp.size() * 8, cudaMemcpyHostToDevice));
+  {
+    // CurrPos before the first step is pos + disp (only used for the grid origin)
+    std::vector<double> cu(tmp.size());
+    for (size_t i = 0; i < tmp.size(); ++i) cu[i] = 0.0;
+    for (uint32_t i = 0; i < N; ++i)
+      for (uint32_t c = 0; c < D; ++c) cu[(size_t)i * S + c] = s->pos[(size_t)i * D + c] + s->disp[(size_t)i * D + c];
+    CU(cudaMemcpy(P.cur, cu.data(), cu.size() * 8, cudaMemcpyHostToDevice));
+  }
+  pack(s->vel);
+  CU(cudaMemcpy(h->vel_a, tmp.data(), tmp.size() * 8, cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(h->vel_b, tmp.data(), tmp.size() * 8, cudaMemcpyHostToDevice));
+  pack(s->acc);
+  CU(cudaMemcpy(P.acc, tmp.data(), tmp.size() * 8, cudaMemcpyHostToDevice));
+  pack(s->extforce);
+  CU(cudaMemcpy(P.extf, tmp.data(), tmp.size() * 8, cudaMemcpyHostToDevice));
+  CU(cudaMemset(P.force, 0, tmp.size() * 8));
+  CU(cudaMemcpy(P.vol, s->vol, (size_t)N * 8, cudaMemcpyHostToDevice));
+
+  // ---- per node metadata ----
+  std::vector<uint32_t> node_grain(N), bdry_rank(N, NONE);
+  std::vector<uint8_t> clamped(N, 0);
+  for (uint32_t g = 0; g < G; ++g) {
+    uint32_t n0 = s->grain_node_offset[g];
+    for (uint32_t i = n0; i < s->grain_node_offset[g + 1]; ++i) node_grain[i] = g;
+    for (uint32_t k = s->bdry_offset[g]; k < s->bdry_offset[g + 1]; ++k) {
+      uint32_t nd = n0 + s->bdry_nodes[k];
+      if (bdry_rank[nd] != NONE) return fail(PG_EINVAL, "duplicate entry in bdry_nodes of grain " + std::to_string(g));
+      bdry_rank[nd] = k - s->bdry_offset[g];
+    }
+    for (uint32_t k = s->clamped_offset[g]; k < s->clamped_offset[g + 1]; ++k) clamped[n0 + s->clamped_nodes[k]] = 1;
+  }
+  CU(h->dalloc(&P.node_grain, N));
+  CU(h->dalloc(&P.bdry_rank, N));
+  CU(h->dalloc(&P.clamped, N));
+  CU(h->dalloc(&P.clamp_pending, N));
+  CU(cudaMemcpy(P.node_grain, node_grain.data(), N * 4, cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(P.bdry_rank, bdry_rank.data(), N * 4, cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(P.clamped, clamped.data(), N, cudaMemcpyHostToDevice));
+  CU(cudaMemset(P.clamp_pending, 0, N));
+
+  // ---- bonds: reference CSR -> SELL-32 ----
+  const uint32_t NC = P.n_chunks;
+  h->node_deg.resize(N);
+  h->chunk_slot.resize(NC + 1);
+  h->chunk_word.resize(NC + 1);
+  std::vector<uint32_t> chunk_deg(NC, 0);
+  for (uint32_t i = 0; i < N; ++i) {
+    h->node_deg[i] = (uint32_t)(s->bond_offset[i + 1] - s->bond_offset[i]);
+    chunk_deg[i >> 5] = std::max<uint32_t>(chunk_deg[i >> 5], h->node_deg[i]);
+  }
+  uint64_t slots = 0, words = 0;
+  for (uint32_t c = 0; c < NC; ++c) {
+    h->chunk_slot[c] = (uint32_t)slots;
+    h->chunk_word[c] = (uint32_t)words;
+    slots += (uint64_t)chunk_deg[c] * 32;
+    words += chunk_deg[c];
+  }
+  h->chunk_slot[NC] = (uint32_t)slots;
+  h->chunk_word[NC] = (uint32_t)words;
+  if (slots >= (1ull << 32)) return fail(PG_EINVAL, "bond slab too large");
+  std::vector<uint32_t> bcol(slots, 0), alive(words, 0);
+  std::vector<double> bxin(slots, 1.0);
+  for (uint32_t i = 0; i < N; ++i) {
+    const uint32_t g = node_grain[i], n0 = s->grain_node_offset[g];
+    const uint32_t c = i >> 5, lane = i & 31;
+    for (uint32_t k = 0; k < h->node_deg[i]; ++k) {
+      const uint64_t b = s->bond_offset[i] + k;
+      const uint32_t j = n0 + s->bond_local[b];
+      const size_t sl = h->chunk_slot[c] + (size_t)k * 32 + lane;
+      bcol[sl] = j;
+      // gen_xi (particle2.h:236-252): xi = pos[j] - pos[i]; xi_norm = |xi|
+      double xi[3];
+      for (uint32_t a = 0; a < D; ++a) xi[a] = s->pos[(size_t)j * D + a] - s->pos[(size_t)i * D + a];
+      double n2 = xi[0] * xi[0];
+      for (uint32_t a = 1; a < D; ++a) n2 = n2 + xi[a] * xi[a];
+      bxin[sl] = std::sqrt(n2);
+      alive[h->chunk_word[c] + k] |= (1u << lane);
+    }
+  }
+  CU(h->dalloc(&P.chunk_slot, NC + 1));
+  CU(h->dalloc(&P.chunk_word, NC + 1));
+  CU(h->dalloc(&P.chunk_deg, NC));
+  CU(h->dalloc(&P.node_deg, N));
+  CU(h->dalloc(&P.bcol, slots));
+  CU(h->dalloc(&P.bxin, slots));
+  CU(h->dalloc(&P.alive, words));
+  CU(h->dalloc(&P.break_step, slots));
+  CU(cudaMemcpy(P.chunk_slot, h->chunk_slot.data(), (NC + 1) * 4, cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(P.chunk_word, h->chunk_word.data(), (NC + 1) * 4, cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(P.chunk_deg, chunk_deg.data(), NC * 4, cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(P.node_deg, h->node_deg.data(), N * 4, cudaMemcpyHostToDevice));
+  if (slots) {
+    CU(cudaMemcpy(P.bcol, bcol.data(), slots * 4, cudaMemcpyHostToDevice));
+    CU(cudaMemcpy(P.bxin, bxin.data(), slots * 8, cudaMemcpyHostToDevice));
+    CU(cudaMemset(P.break_step, 0, slots * 4));
+  }
+  if (words) CU(cudaMemcpy(P.alive, alive.data(), words * 4, cudaMemcpyHostToDevice));
+
+  // ---- grains ----
+  std::vector<GrainDev> grains(G);
+  for (uint32_t g = 0; g < G; ++g) {
+    GrainDev& gd = grains[g];
+    gd.node_begin = s->grain_node_offset[g];
+    gd.node_end = s->grain_node_offset[g + 1];
+    gd.inst = s->grain_instance[g];
+    gd.flags = (s->movable[g] ? GF_MOVABLE : 0) | (s->breakable[g] ? GF_BREAKABLE : 0) |
+               (s->stoppable[g] ? GF_STOPPABLE : 0) | (s->break_bonds[g] ? GF_BREAK_BONDS : 0);
+    gd.rho = s->rho[g];
+    gd.one_over_rho = 1 / s->rho[g];
+    gd.cnot = s->cnot[g];
+    gd.snot = s->snot[g];
+    gd.torque_axis = s->torque_axis ? s->torque_axis[g] : 2;
+    gd.torque_val = s->torque_val ? s->torque_val[g] : 0.0;
+    gd.pad = 0;
+  }
+  CU(h->dalloc(&P.grain, G));
+  CU(cudaMemcpy(P.grain, grains.data(), G * sizeof(GrainDev), cudaMemcpyHostToDevice));
+  CU(h->dalloc(&P.bbox, (size_t)G * 2 * D));
+  {
+    std::vector<unsigned long long> bb((size_t)G * 2 * D);
+    for (size_t i = 0; i < bb.size(); ++i) bb[i] = ((i % (2 * D)) < D) ? ~0ull : 0ull;
+    CU(cudaMemcpy(P.bbox, bb.data(), bb.size() * 8, cudaMemcpyHostToDevice));
+  }
+  CU(h->dalloc(&P.torque_c, (size_t)G * 3));
+  CU(cudaMemset(P.torque_c, 0, (size_t)G * 3 * 8));
+
+  // ---- instances: contact parameters, wall, hashed grid ----
+  h->inst_host.resize(I);
+  uint64_t table_total = 0;
+  for (uint32_t k = 0; k < I; ++k) {
+    InstDev& in = h->inst_host[k];
+    std::memset(&in, 0, sizeof(in));
+    in.contact_rad = s->contact_radius[k];
+    in.normal_stiffness = s->normal_stiffness[k];
+    in.friction_coefficient = s->friction_coefficient[k];
+    in.damping_ratio = s->damping_ratio[k];
+    in.allow_wall = s->allow_wall[k];
+    for (uint32_t a = 0; a < 2 * D; ++a) {
+      in.wall[a] = s->wall_geom[(size_t)k * 2 * D + a];
+      in.wall_speed[a] = s->wall_speed[(size_t)k * 2 * D + a];
+    }
+    in.node_begin = NONE;
+    in.node_end = 0;
+  }
+  for (uint32_t g = 0; g < G; ++g) {
+    InstDev& in = h->inst_host[s->grain_instance[g]];
+    in.node_begin = std::min(in.node_begin, s->grain_node_offset[g]);
+    in.node_end = std::max(in.node_end, s->grain_node_offset[g + 1]);
+  }
+  for (uint32_t k = 0; k < I; ++k) {
+    InstDev& in = h->inst_host[k];
+    if (in.node_begin == NONE) {  // instance without grains
+      in.node_begin = in.node_end = 0;
+    }
+    double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (uint32_t i = in.node_begin; i < in.node_end; ++i)
+      for (uint32_t a = 0; a < D; ++a) {
+        double x = s->pos[(size_t)i * D + a] + s->disp[(size_t)i * D + a];
+        lo[a] = std::min(lo[a], x);
+        hi[a] = std::max(hi[a], x);
+      }
+    double ext = 0;
+    for (uint32_t a = 0; a < D; ++a) {
+      if (!std::isfinite(lo[a])) lo[a] = hi[a] = 0;
+      in.origin[a] = 0.5 * (lo[a] + hi[a]);
+      ext = std::max(ext, hi[a] - lo[a]);
+    }
+    double cell = in.contact_rad * 1.0625;
+    if (!(cell > 0) || !std::isfinite(cell)) cell = std::max(ext, 1e-9) / 64;
+    in.cell = cell;
+    in.cell_f = (float)cell;
+    in.inv_cell_f = (float)(1.0 / cell);
+    in.range_f = (float)(cell * 262144.0);
+    const uint32_t nn = in.node_end - in.node_begin;
+    const uint32_t T = next_pow2(std::max<uint64_t>(64, 2ull * nn));
+    in.table_off = (uint32_t)table_total;
+    in.table_mask = T - 1;
+    table_total += T;
+  }
+  if (table_total >= (1ull << 31)) return fail(PG_EINVAL, "grid table too large");
+  P.table_total = (uint32_t)table_total;
+  CU(h->dalloc(&P.inst, I));
+  CU(cudaMemcpy(P.inst, h->inst_host.data(), I * sizeof(InstDev), cudaMemcpyHostToDevice));
+  CU(h->dalloc(&P.reaction, (size_t)I * 2 * D * D));
+  CU(cudaMemset(P.reaction, 0, (size_t)I * 2 * D * D * 8));
+
+  // ---- grid buffers ----
+  CU(h->dalloc(&P.cell_key, N));
+  CU(h->dalloc(&P.cell_rank, N));
+  CU(h->dalloc(&P.sorted, N));
+  CU(h->dalloc(&P.cell_count, table_total));
+  CU(h->dalloc(&P.cell_start, table_total + 1));
+  CU(cudaMemset(P.cell_count, 0, table_total * 4));
+  const uint32_t ntiles = (uint32_t)((table_total + 4095) / 4096);
+  CU(h->dalloc(&P.scan_tile_sum, ntiles));
+  CU(h->dalloc(&P.scan_done, 1));
+  CU(cudaMemset(P.scan_done, 0, 4));
+
+  // ---- wall records, logs, control ----
+  P.wrec_cap = (uint32_t)std::min<uint64_t>(WREC_SMEM_CAP, 2ull * D * N);
+  CU(h->dalloc(&P.wrec, P.wrec_cap));
+  CU(h->dalloc(&P.wrec_count, 1));
+  CU(cudaMemset(P.wrec_count, 0, 4));
+  P.log_cap = cfg.pair_log_capacity;
+  CU(h->dalloc(&P.pair_acc, 2));
+  CU(h->dalloc(&P.log_count, P.log_cap));
+  CU(h->dalloc(&P.log_hash, P.log_cap));
+  CU(cudaMemset(P.pair_acc, 0, 16));
+  CU(cudaMemset(P.log_count, 0, (size_t)P.log_cap * 8));
+  CU(cudaMemset(P.log_hash, 0, (size_t)P.log_cap * 8));
+  CU(h->dalloc(&P.step, 1));
+  uint32_t t0 = (uint32_t)h->next_t;
+  CU(cudaMemcpy(P.step, &t0, 4, cudaMemcpyHostToDevice));
+  CU(h->dalloc(&P.status, 1));
+  CU(cudaMemset(P.status, 0, 4));
+  CU(h->dalloc(&P.too_close, 1));
+  CU(cudaMemset(P.too_close, 0, 8));
+  CU(cudaEventCreate(&h->ev_t0));
+  CU(cudaEventCreate(&h->ev_t1));
+  CU(cudaDeviceSynchronize());
+  rc = build_graphs(h.get());
+  if (rc) return rc;
+  *out = h.release();
+  return PG_OK;
+}
+
+int pg_destroy(pg_handle* h) {
+  delete h;
+  return PG_OK;
+}
+
+static int check_device_status(pg_handle* h) {
+  int32_t st = 0;
+  CU(cudaMemcpyAsync(&st, h->P.status, 4, cudaMemcpyDeviceToHost, h->stream));
+  CU(cudaStreamSynchronize(h->stream));
+  if (st) {
+    std::string m = "device reported: ";
+    m += pg_status_string(st);
+    if (st == PG_ECAPACITY) m += " (contact candidates per node, or wall records per step)";
+    return fail(st, m);
+  }
+  return PG_OK;
+}
+
+int pg_step(pg_handle* h, uint32_t nsteps) {
+  if (!h) return fail(PG_EINVAL, "null handle");
+  uint64_t launches = 0;
+  if (h->timing) {
+    // timed mode: plain launches with CUDA events around every force kernel
+    if (h->ev.size() < 2 * (size_t)nsteps) {
+      size_t old = h->ev.size();
+      h->ev.resize(2 * (size_t)nsteps);
+      for (size_t i = old; i < h->ev.size(); ++i) CU(cudaEventCreate(&h->ev[i]));
+    }
+    h->force_ms = 0;
+    h->force_launches = 0;
+    CU(cudaEventRecord(h->ev_t0, h->stream));
+    for (uint32_t k = 0; k < nsteps; ++k) {
+      Dev P = h->P;
+      set_vel(h, P, h->vel_parity);
+      launch_step_timed(P, h->L, h->stream, &launches, h->ev[2 * k], h->ev[2 * k + 1]);
+      h->vel_parity ^= 1;
+    }
+    CU(cudaEventRecord(h->ev_t1, h->stream));
+    CU(cudaEventSynchronize(h->ev_t1));
+    for (uint32_t k = 0; k < nsteps; ++k) {
+      float ms = 0;
+      CU(cudaEventElapsedTime(&ms, h->ev[2 * k], h->ev[2 * k + 1]));
+      h->force_ms += ms;
+    }
+    float tot = 0;
+    CU(cudaEventElapsedTime(&tot, h->ev_t0, h->ev_t1));
+    h->total_ms = tot;
+    h->force_launches = nsteps;
+  } else {
+    uint32_t k = 0;
+    while (k < nsteps) {
+      if (nsteps - k >= (uint32_t)pg_handle::GRAPH_STEPS) {
+        CU(cudaGraphLaunch(h->graph[h->vel_parity], h->stream));
+        launches += h->graph_launches_per;
+        k += pg_handle::GRAPH_STEPS;  // GRAPH_STEPS is even: parity unchanged
+      } else {
+        enqueue_step(h, h->vel_parity, &launches);
+        h->vel_parity ^= 1;
+        ++k;
+      }
+    }
+    CU(cudaGetLastError());
+  }
+  h->next_t += nsteps;
+  h->last_launches = launches;
+  return PG_OK;
+}
+
+int pg_synchronize(pg_handle* h) {
+  if (!h) return fail(PG_EINVAL, "null handle");
+  CU(cudaStreamSynchronize(h->stream));
+  return check_device_status(h);
+}
+
+int pg_get_step(pg_handle* h, uint64_t* t) {
+  if (!h || !t) return fail(PG_EINVAL, "null argument");
+  *t = h->next_t;
+  return PG_OK;
+}
+
+static double* field_ptr(pg_handle* h, int field) {
+  switch (field) {
+    case PG_FIELD_CURRPOS: return h->P.cur;
+    case PG_FIELD_VEL: return h->vel_parity == 0 ? h->vel_a : h->vel_b;
+    case PG_FIELD_ACC: return h->P.acc;
+    case PG_FIELD_FORCE: return h->P.force;
+    case PG_FIELD_DISP: return h->P.disp;
+    case PG_FIELD_POS: return h->P.pos;
+  }
+  return nullptr;
+}
+
+int pg_get_field(pg_handle* h, int field, double* out) {
+  if (!h || !out) return fail(PG_EINVAL, "null argument");
+  double* src = field_ptr(h, field);
+  if (!src) return fail(PG_EINVAL, "unknown field");
+  int rc = pg_synchronize(h);
+  if (rc) return rc;
+  const uint32_t N = h->P.N, D = h->dim, S = h->S;
+  std::vector<double> tmp((size_t)N * S);
+  CU(cudaMemcpy(tmp.data(), src, tmp.size() * 8, cudaMemcpyDeviceToHost));
+  for (uint32_t i = 0; i < N; ++i)
+    for (uint32_t c = 0; c < D; ++c) out[(size_t)i * D + c] = tmp[(size_t)i * S + c];
+  if (field == PG_FIELD_DISP) {
+    std::vector<uint8_t> pend(N);
+    CU(cudaMemcpy(pend.data(), h->P.clamp_pending, N, cudaMemcpyDeviceToHost));
+    for (uint32_t i = 0; i < N; ++i)
+      if (pend[i])
+        for (uint32_t c = 0; c < D; ++c) out[(size_t)i * D + c] = 0.0;
+  }
+  return PG_OK;
+}
+
+int pg_set_field(pg_handle* h, int field, const double* in) {
+  if (!h || !in) return fail(PG_EINVAL, "null argument");
+  int rc = pg_synchronize(h);
+  if (rc) return rc;
+  const uint32_t N = h->P.N, D = h->dim, S = h->S;
+  if (field == PG_FIELD_POS && !h->xpos_separate) {
+    // keep the bond reference positions (xi = pos[j] - pos[i] at load time) unchanged
+    double* x = nullptr;
+    CU(cudaMalloc((void**)&x, (size_t)N * S * 8));
+    CU(cudaMemcpy(x, h->P.pos, (size_t)N * S * 8, cudaMemcpyDeviceToDevice));
+    h->P.xpos = x;
+    h->xpos_separate = true;
+    rc = build_graphs(h);
+    if (rc) return rc;
+  }
+  double* dst = nullptr;
+  switch (field) {
+    case PG_FIELD_POS: dst = h->P.pos; break;
+    case PG_FIELD_DISP: dst = h->P.disp; break;
+    case PG_FIELD_VEL: dst = h->vel_parity == 0 ? h->vel_a : h->vel_b; break;
+    case PG_FIELD_ACC: dst = h->P.acc; break;
+    default: return fail(PG_EINVAL, "field not writable");
+  }
+  std::vector<double> tmp((size_t)N * S, 0.0);
+  for (uint32_t i = 0; i < N; ++i)
+    for (uint32_t c = 0; c < D; ++c) tmp[(size_t)i * S + c] = in[(size_t)i * D + c];
+  CU(cudaMemcpy(dst, tmp.data(), tmp.size() * 8, cudaMemcpyHostToDevice));
+  if (field == PG_FIELD_DISP) CU(cudaMemset(h->P.clamp_pending, 0, N));
+  return PG_OK;
+}
+
+int pg_get_bond_alive(pg_handle* h, uint8_t* out) {
+  if (!h || !out) return fail(PG_EINVAL, "null argument");
+  int rc = pg_synchronize(h);
+  if (rc) return rc;
+  const uint32_t N = h->P.N, NC = h->P.n_chunks;
+  std::vector<uint32_t> words(h->chunk_word[NC]);
+  if (!words.empty()) CU(cudaMemcpy(words.data(), h->P.alive, words.size() * 4, cudaMemcpyDeviceToHost));
+  for (uint32_t i = 0; i < N; ++i) {
+    const uint32_t c = i >> 5, lane = i & 31;
+    for (uint32_t k = 0; k < h->node_deg[i]; ++k)
+      out[h->bond_offset[i] + k] = (words[h->chunk_word[c] + k] >> lane) & 1u;
+  }
+  return PG_OK;
+}
+
+int pg_get_bond_break_step(pg_handle* h, uint32_t* out) {
+  if (!h || !out) return fail(PG_EINVAL, "null argument");
+  int rc = pg_synchronize(h);
+  if (rc) return rc;
+  const uint32_t N = h->P.N, NC = h->P.n_chunks;
+  std::vector<uint32_t> bs(h->chunk_slot[NC]);
+  if (!bs.empty()) CU(cudaMemcpy(bs.data(), h->P.break_step, bs.size() * 4, cudaMemcpyDeviceToHost));
+  for (uint32_t i = 0; i < N; ++i) {
+    const uint32_t c = i >> 5, lane = i & 31;
+    for (uint32_t k = 0; k < h->node_deg[i]; ++k)
+      out[h->bond_offset[i] + k] = bs[h->chunk_slot[c] + (size_t)k * 32 + lane];
+  }
+  return PG_OK;
+}
+
+int pg_set_bond_alive(pg_handle* h, const uint8_t* in) {
+  if (!h || !in) return fail(PG_EINVAL, "null argument");
+  int rc = pg_synchronize(h);
+  if (rc) return rc;
+  const uint32_t N = h->P.N, NC = h->P.n_chunks;
+  std::vector<uint32_t> words(h->chunk_word[NC], 0);
+  for (uint32_t i = 0; i < N; ++i) {
+    const uint32_t c = i >> 5, lane = i & 31;
+    for (uint32_t k = 0; k < h->node_deg[i]; ++k)
+      if (in[h->bond_offset[i] + k]) words[h->chunk_word[c] + k] |= 1u << lane;
+  }
+  if (!words.empty()) CU(cudaMemcpy(h->P.alive, words.data(), words.size() * 4, cudaMemcpyHostToDevice));
+  return PG_OK;
+}
+
+int pg_get_reaction(pg_handle* h, double* out) {
+  if (!h || !out) return fail(PG_EINVAL, "null argument");
+  int rc = pg_synchronize(h);
+  if (rc) return rc;
+  CU(cudaMemcpy(out, h->P.reaction, (size_t)h->P.I * 2 * h->dim * h->dim * 8, cudaMemcpyDeviceToHost));
+  return PG_OK;
+}
+
+int pg_get_wall(pg_handle* h, double* out) {
+  if (!h || !out) return fail(PG_EINVAL, "null argument");
+  int rc = pg_synchronize(h);
+  if (rc) return rc;
+  std::vector<InstDev> in(h->P.I);
+  CU(cudaMemcpy(in.data(), h->P.inst, in.size() * sizeof(InstDev), cudaMemcpyDeviceToHost));
+  const uint32_t NS = 2 * h->dim;
+  for (uint32_t k = 0; k < h->P.I; ++k)
+    for (uint32_t a = 0; a < NS; ++a) out[(size_t)k * NS + a] = in[k].wall[a];
+  return PG_OK;
+}
+
+int pg_set_wall(pg_handle* h, const double* geom) {
+  if (!h || !geom) return fail(PG_EINVAL, "null argument");
+  int rc = pg_synchronize(h);
+  if (rc) return rc;
+  std::vector<InstDev> in(h->P.I);
+  CU(cudaMemcpy(in.data(), h->P.inst, in.size() * sizeof(InstDev), cudaMemcpyDeviceToHost));
+  const uint32_t NS = 2 * h->dim;
+  for (uint32_t k = 0; k < h->P.I; ++k)
+    for (uint32_t a = 0; a < NS; ++a) in[k].wall[a] = geom[(size_t)k * NS + a];
+  CU(cudaMemcpy(h->P.inst, in.data(), in.size() * sizeof(InstDev), cudaMemcpyHostToDevice));
+  return PG_OK;
+}
+
+int pg_set_grain_flags(pg_handle* h, uint32_t grain, int32_t movable, int32_t stoppable) {
+  if (!h || grain >= h->P.G) return fail(PG_EINVAL, "bad grain");
+  int rc = pg_synchronize(h);
+  if (rc) return rc;
+  GrainDev gd;
+  CU(cudaMemcpy(&gd, h->P.grain + grain, sizeof(gd), cudaMemcpyDeviceToHost));
+  if (movable >= 0) gd.flags = movable ? (gd.flags | GF_MOVABLE) : (gd.flags & ~GF_MOVABLE);
+  if (stoppable >= 0) gd.flags = stoppable ? (gd.flags | GF_STOPPABLE) : (gd.flags & ~GF_STOPPABLE);
+  CU(cudaMemcpy(h->P.grain + grain, &gd, sizeof(gd), cudaMemcpyHostToDevice));
+  return PG_OK;
+}
+
+int pg_get_pair_log(pg_handle* h, uint32_t n, uint64_t* count, uint64_t* hash) {
+  if (!h || !count || !hash) return fail(PG_EINVAL, "null argument");
+  if (n > h->P.log_cap) return fail(PG_EINVAL, "n exceeds the pair log capacity");
+  int rc = pg_synchronize(h);
+  if (rc) return rc;
+  std::vector<unsigned long long> c(h->P.log_cap), hs(h->P.log_cap);
+  CU(cudaMemcpy(c.data(), h->P.log_count, c.size() * 8, cudaMemcpyDeviceToHost));
+  CU(cudaMemcpy(hs.data(), h->P.log_hash, hs.size() * 8, cudaMemcpyDeviceToHost));
+  // last completed step is next_t - 1; entry of step t sits at (t - 1) % cap
+  for (uint32_t k = 0; k < n; ++k) {
+    uint64_t t = h->next_t - n + k;
+    if (t < 1) {
+      count[k] = 0;
+      hash[k] = 0;
+      continue;
+    }
+    uint32_t slot = (uint32_t)((t - 1) % h->P.log_cap);
+    count[k] = c[slot];
+    hash[k] = hs[slot];
+  }
+  return PG_OK;
+}
+
+int pg_get_device_status(pg_handle* h, int32_t* status, uint64_t* too_close) {
+  if (!h) return fail(PG_EINVAL, "null handle");
+  CU(cudaStreamSynchronize(h->stream));
+  int32_t st = 0;
+  unsigned long long tc = 0;
+  CU(cudaMemcpy(&st, h->P.status, 4, cudaMemcpyDeviceToHost));
+  CU(cudaMemcpy(&tc, h->P.too_close, 8, cudaMemcpyDeviceToHost));
+  if (status) *status = st;
+  if (too_close) *too_close = tc;
+  return PG_OK;
+}
+
+int pg_get_launch_count(pg_handle* h, uint64_t* n) {
+  if (!h || !n) return fail(PG_EINVAL, "null argument");
+  *n = h->last_launches;
+  return PG_OK;
+}
+
+int pg_set_timing(pg_handle* h, int32_t enable) {
+  if (!h) return fail(PG_EINVAL, "null handle");
+  h->timing = enable != 0;
+  return PG_OK;
+}
+
+int pg_get_kernel_times(pg_handle* h, double* force_ms, double* total_ms, uint64_t* force_launches) {
+  if (!h) return fail(PG_EINVAL, "null handle");
+  if (force_ms) *force_ms = h->force_ms;
+  if (total_ms) *total_ms = h->total_ms;
+  if (force_launches) *force_launches = h->force_launches;
+  return PG_OK;
+}
+
+}  // extern "C"

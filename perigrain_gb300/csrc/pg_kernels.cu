@@ -1,0 +1,848 @@
+// GB300 (sm_103a) kernels of the PeriDEM time step, FP64 parity path.
+//
+// One step (reference src/particle/timeloop.h:608-879) is six launches on one stream:
+//   k_predict      position update (timeloop.h:661-669) + grid key + per-grain bounding box
+//   k_scan_reduce  \ exclusive scan of the per-bucket counts = cell-start table
+//   k_scan_final   /
+//   k_scatter      nodes -> bucket order (counting sort, one digit spanning all buckets)
+//   k_force        bond force + break (particle2.h:102-232), self/inter-grain contact
+//                  (contact.h:668-812), wall (contact.h:900-964, :314-431, :16-41),
+//                  external force and torque (timeloop.h:774-824), velocity update
+//                  (timeloop.h:834-863) -- fused, one node per thread
+//   k_finalize     ordered wall-reaction sums, pair log, wall move (timeloop.h:866-878)
+//
+// This file is compiled with --fmad=false: every FP64 operation is the IEEE operation the
+// reference performs, in the reference's order, so the non-wall path is bit-exact.
+#include <cuda_runtime.h>
+
+#include <cmath>
+
+#include "pg_device.cuh"
+#include "pg_kernels.h"
+
+namespace pg {
+
+template <int D>
+struct Lay {
+  static constexpr int S = (D == 2) ? 2 : 4;   // doubles per node vector
+  static constexpr int SF = (D == 2) ? 2 : 4;  // floats per node vector (curf)
+};
+
+template <int D>
+__device__ __forceinline__ void ldv(const double* a, uint32_t i, double (&v)[D]) {
+  if constexpr (D == 2) {
+    double2 t = reinterpret_cast<const double2*>(a)[i];
+    v[0] = t.x;
+    v[1] = t.y;
+  } else {
+    const double2* p = reinterpret_cast<const double2*>(a + 4ull * i);
+    double2 t0 = p[0], t1 = p[1];
+    v[0] = t0.x;
+    v[1] = t0.y;
+    v[2] = t1.x;
+  }
+}
+template <int D>
+__device__ __forceinline__ void stv(double* a, uint32_t i, const double (&v)[D]) {
+  if constexpr (D == 2) {
+    reinterpret_cast<double2*>(a)[i] = make_double2(v[0], v[1]);
+  } else {
+    double2* p = reinterpret_cast<double2*>(a + 4ull * i);
+    p[0] = make_double2(v[0], v[1]);
+    p[1] = make_double2(v[2], 0.0);
+  }
+}
+template <int D>
+__device__ __forceinline__ void ldf(const float* a, uint32_t i, float (&v)[D]) {
+  if constexpr (D == 2) {
+    float2 t = reinterpret_cast<const float2*>(a)[i];
+    v[0] = t.x;
+    v[1] = t.y;
+  } else {
+    float4 t = reinterpret_cast<const float4*>(a)[i];
+    v[0] = t.x;
+    v[1] = t.y;
+    v[2] = t.z;
+  }
+}
+
+__device__ __forceinline__ void set_status(int32_t* st, int32_t code) { atomicCAS(st, 0, code); }
+
+// ---------------------------------------------------------------------------------------------
+// k_predict: disp += dt*vel + (dt*dt*0.5)*acc for movable grains; CurrPos = pos + disp.
+// ---------------------------------------------------------------------------------------------
+template <int D>
+__global__ void __launch_bounds__(256) k_predict(const Dev P) {
+  const uint32_t d = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t lane = threadIdx.x & 31;
+  const bool act = d < P.N;
+  uint32_t g = 0;
+  unsigned long long kmin[D], kmax[D];
+  if (act) {
+    g = P.node_grain[d];
+    const GrainDev& gr = P.grain[g];
+    double dp[D], ps[D], cu[D];
+    ldv<D>(P.disp, d, dp);
+    bool wrote = false;
+    if (P.clamp_pending[d]) {
+      // a clamped node zeroed at the end of the previous step (timeloop.h:854-860)
+      for (int c = 0; c < D; ++c) dp[c] = 0.0;
+      P.clamp_pending[d] = 0;
+      wrote = true;
+    }
+    if (gr.flags & GF_MOVABLE) {
+      double v[D], a[D];
+      ldv<D>(P.vel_in, d, v);
+      ldv<D>(P.acc, d, a);
+      for (int c = 0; c < D; ++c) dp[c] = dp[c] + ((P.dt * v[c]) + (P.hdt2 * a[c]));
+      wrote = true;
+    }
+    if (wrote) stv<D>(P.disp, d, dp);
+    ldv<D>(P.pos, d, ps);
+    for (int c = 0; c < D; ++c) cu[c] = ps[c] + dp[c];
+    stv<D>(P.cur, d, cu);
+
+    // grid key from the FP32 offset to the instance origin
+    const InstDev& in = P.inst[gr.inst];
+    float rf[4] = {0.f, 0.f, 0.f, 0.f};
+    int32_t ci[3] = {0, 0, 0};
+    bool ok = true;
+    for (int c = 0; c < D; ++c) {
+      if (!isfinite(cu[c])) ok = false;
+      rf[c] = (float)(cu[c] - in.origin[c]);
+      if (!(fabsf(rf[c]) <= in.range_f)) ok = false;
+      ci[c] = (int32_t)floorf(rf[c] * in.inv_cell_f);
+    }
+    if (!ok) {
+      set_status(P.status, isfinite(cu[0] + cu[1] + (D == 3 ? cu[D - 1] : 0.0)) ? PG_ERANGE : PG_ENAN);
+      for (int c = 0; c < D; ++c) ci[c] = 0;
+    }
+    if constexpr (D == 2) {
+      reinterpret_cast<float2*>(P.curf)[d] = make_float2(rf[0], rf[1]);
+    } else {
+      reinterpret_cast<float4*>(P.curf)[d] = make_float4(rf[0], rf[1], rf[2], 0.f);
+    }
+    uint32_t m = (D == 2) ? morton2((uint32_t)ci[0], (uint32_t)ci[1])
+                          : morton3((uint32_t)ci[0], (uint32_t)ci[1], (uint32_t)ci[2]);
+    uint32_t key = in.table_off + (m & in.table_mask);
+    P.cell_key[d] = key;
+    P.cell_rank[d] = atomicAdd(&P.cell_count[key], 1u);
+    for (int c = 0; c < D; ++c) {
+      kmin[c] = dbl_to_ordered(cu[c]);
+      kmax[c] = kmin[c];
+    }
+  } else {
+    for (int c = 0; c < D; ++c) {
+      kmin[c] = ~0ull;
+      kmax[c] = 0ull;
+    }
+  }
+  // per-grain bounding box (contact.h:1024-1062), min/max are exact so atomics are deterministic
+  const uint32_t full = 0xffffffffu;
+  uint32_t g0 = __shfl_sync(full, g, 0);
+  bool lane0_act = __shfl_sync(full, act ? 1 : 0, 0);
+  if (!lane0_act) return;
+  uint32_t same = __ballot_sync(full, !act || g == g0);
+  if (same == full) {
+    for (int c = 0; c < D; ++c) {
+      for (int off = 16; off > 0; off >>= 1) {
+        unsigned long long o1 = __shfl_down_sync(full, kmin[c], off);
+        unsigned long long o2 = __shfl_down_sync(full, kmax[c], off);
+        kmin[c] = o1 < kmin[c] ? o1 : kmin[c];
+        kmax[c] = o2 > kmax[c] ? o2 : kmax[c];
+      }
+    }
+    if (lane == 0) {
+      for (int c = 0; c < D; ++c) {
+        atomicMin(&P.bbox[(size_t)g0 * 2 * D + c], kmin[c]);
+        atomicMax(&P.bbox[(size_t)g0 * 2 * D + D + c], kmax[c]);
+      }
+    }
+  } else if (act) {
+    for (int c = 0; c < D; ++c) {
+      atomicMin(&P.bbox[(size_t)g * 2 * D + c], kmin[c]);
+      atomicMax(&P.bbox[(size_t)g * 2 * D + D + c], kmax[c]);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Exclusive scan of cell_count -> cell_start (reduce-then-scan, last block scans tile sums).
+// ---------------------------------------------------------------------------------------------
+constexpr int SCAN_THREADS = 1024;
+constexpr int SCAN_PER = 4;
+constexpr int SCAN_TILE = SCAN_THREADS * SCAN_PER;
+
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* warp_sums, uint32_t* total) {
+  const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  uint32_t x = v;
+  for (int off = 1; off < 32; off <<= 1) {
+    uint32_t y = __shfl_up_sync(0xffffffffu, x, off);
+    if (lane >= (uint32_t)off) x += y;
+  }
+  if (lane == 31) warp_sums[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    uint32_t nw = blockDim.x >> 5;
+    uint32_t s = lane < nw ? warp_sums[lane] : 0;
+    for (int off = 1; off < 32; off <<= 1) {
+      uint32_t y = __shfl_up_sync(0xffffffffu, s, off);
+      if (lane >= (uint32_t)off) s += y;
+    }
+    if (lane < nw) warp_sums[lane] = s;
+  }
+  __syncthreads();
+  uint32_t base = wid ? warp_sums[wid - 1] : 0;
+  if (total) *total = warp_sums[(blockDim.x >> 5) - 1];
+  return base + x - v;
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(const Dev P) {
+  __shared__ uint32_t ws[32];
+  __shared__ bool last;
+  const uint32_t tile = blockIdx.x;
+  const uint32_t base = tile * SCAN_TILE + threadIdx.x * SCAN_PER;
+  uint32_t s = 0;
+  for (int k = 0; k < SCAN_PER; ++k) {
+    uint32_t i = base + k;
+    if (i < P.table_total) s += P.cell_count[i];
+  }
+  uint32_t tot;
+  block_excl_scan(s, ws, &tot);
+  if (threadIdx.x == 0) {
+    P.scan_tile_sum[tile] = tot;
+    __threadfence();
+    uint32_t ticket = atomicAdd(P.scan_done, 1u);
+    last = (ticket == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  // last block: exclusive scan of the tile sums in place
+  const uint32_t ntiles = gridDim.x;
+  uint32_t carry = 0;
+  for (uint32_t b0 = 0; b0 < ntiles; b0 += SCAN_THREADS) {
+    uint32_t i = b0 + threadIdx.x;
+    uint32_t v = i < ntiles ? ((volatile uint32_t*)P.scan_tile_sum)[i] : 0;
+    uint32_t t2;
+    uint32_t ex = block_excl_scan(v, ws, &t2);
+    __syncthreads();
+    if (i < ntiles) P.scan_tile_sum[i] = carry + ex;
+    carry += t2;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *P.scan_done = 0;
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_final(const Dev P) {
+  __shared__ uint32_t ws[32];
+  const uint32_t tile = blockIdx.x;
+  const uint32_t base = tile * SCAN_TILE + threadIdx.x * SCAN_PER;
+  uint32_t v[SCAN_PER];
+  uint32_t s = 0;
+  for (int k = 0; k < SCAN_PER; ++k) {
+    uint32_t i = base + k;
+    v[k] = i < P.table_total ? P.cell_count[i] : 0;
+    s += v[k];
+  }
+  uint32_t ex = block_excl_scan(s, ws, nullptr) + P.scan_tile_sum[tile];
+  for (int k = 0; k < SCAN_PER; ++k) {
+    uint32_t i = base + k;
+    if (i < P.table_total) {
+      P.cell_start[i] = ex;
+      P.cell_count[i] = 0;  // ready for the next step's counting pass
+    }
+    ex += v[k];
+  }
+  if (tile == gridDim.x - 1 && threadIdx.x == blockDim.x - 1) P.cell_start[P.table_total] = P.N;
+}
+
+__global__ void __launch_bounds__(256) k_scatter(const Dev P) {
+  const uint32_t d = blockIdx.x * blockDim.x + threadIdx.x;
+  if (d < P.N) P.sorted[P.cell_start[P.cell_key[d]] + P.cell_rank[d]] = d;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Torque centroid: mean_CurrPos (particle2.h:89-98) in the reference's serial order.
+// ---------------------------------------------------------------------------------------------
+template <int D>
+__global__ void k_torque_center(const Dev P) {
+  const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= P.G) return;
+  const GrainDev gr = P.grain[g];
+  double m[D];
+  for (int c = 0; c < D; ++c) m[c] = 0.0;
+  for (uint32_t i = gr.node_begin; i < gr.node_end; ++i) {
+    double cu[D];
+    ldv<D>(P.cur, i, cu);
+    for (int c = 0; c < D; ++c) m[c] = m[c] + cu[c];
+  }
+  double n = (double)(gr.node_end - gr.node_begin);
+  for (int c = 0; c < D; ++c) P.torque_c[(size_t)g * 3 + c] = m[c] / n;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Fused force + integrate kernel (FP64 parity).
+// ---------------------------------------------------------------------------------------------
+template <int D>
+__device__ __forceinline__ void grain_box(const Dev& P, uint32_t g, double (&mn)[D], double (&mx)[D]) {
+  for (int c = 0; c < D; ++c) {
+    mn[c] = ordered_to_dbl(P.bbox[(size_t)g * 2 * D + c]);
+    mx[c] = ordered_to_dbl(P.bbox[(size_t)g * 2 * D + D + c]);
+  }
+}
+
+// intersects_box_fext (contact.h:984-1020), written per axis: (min_i - c <= max_j) && (max_i + c >= min_j)
+template <int D>
+__device__ __forceinline__ bool boxes_touch(const double (&mni)[D], const double (&mxi)[D],
+                                            const double (&mnj)[D], const double (&mxj)[D], double c) {
+  bool r = true;
+  for (int a = 0; a < D; ++a) r = r && ((mni[a] - c) <= mxj[a]) && ((mxi[a] + c) >= mnj[a]);
+  return r;
+}
+
+// within_interior_fext (contact.h:1066-1080) applied to get_minmax() and RectWall::lrtb()
+// arrays exactly as the reference indexes them (in 3D this reads the 6-entry arrays with the
+// 2D index pattern, as the reference does).
+template <int D>
+__device__ __forceinline__ bool within_interior(const double (&mn)[D], const double (&mx)[D],
+                                                const double* W, double c) {
+  double A[4];
+  if constexpr (D == 2) {
+    A[0] = mn[0]; A[1] = mx[0]; A[2] = mx[1]; A[3] = mn[1];
+  } else {
+    A[0] = mn[0]; A[1] = mn[1]; A[2] = mn[2]; A[3] = mx[0];
+  }
+  double AL = A[0] - c, AR = A[1] + c, AT = A[2] + c, AB = A[3] - c;
+  return (W[0] < AL) && (AR < W[1]) && (W[2] > AT) && (W[3] < AB);
+}
+
+template <int D>
+__device__ __forceinline__ void insert_cand(unsigned long long (&keys)[MAX_CAND], uint32_t (&idx)[MAX_CAND],
+                                            int& n, unsigned long long key, uint32_t q, const Dev& P) {
+  if (n >= (int)P.max_cand) {
+    set_status(P.status, PG_ECAPACITY);
+    return;
+  }
+  int k = n++;
+  while (k > 0 && keys[k - 1] > key) {
+    keys[k] = keys[k - 1];
+    idx[k] = idx[k - 1];
+    --k;
+  }
+  keys[k] = key;
+  idx[k] = q;
+}
+
+template <int D>
+__global__ void __launch_bounds__(128) k_force(const Dev P) {
+  const uint32_t d = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t chunk = d >> 5;
+  if (chunk >= P.n_chunks) return;  // uniform per warp
+  const bool act = d < P.N;
+  const uint32_t t = *P.step;
+  const uint32_t g = act ? P.node_grain[d] : 0;
+  const GrainDev gr = P.grain[g];
+  const bool mov = act && (gr.flags & GF_MOVABLE);
+  const bool brk = P.enable_fracture && (gr.flags & GF_BREAKABLE) && (gr.flags & GF_BREAK_BONDS);
+
+  double f[D];
+  for (int c = 0; c < D; ++c) f[c] = 0.0;
+  double vp[D];
+  if (act) ldv<D>(P.vel_in, d, vp);
+
+  // ---- bond force and bond breaking (particle2.h:102-150, :191-232) ----
+  const uint32_t cdeg = P.chunk_deg[chunk];
+  const uint32_t slot0 = P.chunk_slot[chunk] + lane;
+  const uint32_t w0 = P.chunk_word[chunk];
+  {
+    double dp[D], xp[D];
+    if (mov) {
+      ldv<D>(P.disp, d, dp);
+      ldv<D>(P.xpos, d, xp);
+    }
+    for (uint32_t k = 0; k < cdeg; ++k) {
+      const uint32_t word = P.alive[w0 + k];
+      bool bit = (word >> lane) & 1u;
+      if (mov && bit) {
+        const uint32_t s = slot0 + 32u * k;
+        const uint32_t j = P.bcol[s];
+        const double xin = P.bxin[s];
+        double dj[D], xj[D];
+        ldv<D>(P.disp, j, dj);
+        ldv<D>(P.xpos, j, xj);
+        double e[D];
+        for (int c = 0; c < D; ++c) e[c] = (dj[c] - dp[c]) + (xj[c] - xp[c]);
+        double n2 = e[0] * e[0];
+        for (int c = 1; c < D; ++c) n2 = n2 + e[c] * e[c];
+        const double en = sqrt(n2);
+        const double str = (en - xin) / xin;
+        const double sc = (gr.cnot * str) * P.vol[j];
+        for (int c = 0; c < D; ++c) f[c] = f[c] + sc * (e[c] / en);
+        if (brk && str > gr.snot) {
+          bit = false;
+          P.break_step[s] = t;
+        }
+      }
+      const uint32_t nw = __ballot_sync(0xffffffffu, bit);
+      if (lane == 0 && nw != word) P.alive[w0 + k] = nw;
+    }
+  }
+  __syncwarp();
+
+  unsigned long long my_pairs = 0, my_hash = 0, my_close = 0;
+  const InstDev& in = P.inst[gr.inst];
+  const bool p_bdry = !P.nl_bdry_only || (act && P.bdry_rank[d] != NONE);
+  const bool selfc = mov && P.enable_fracture && (gr.flags & GF_BREAKABLE) && P.self_contact;
+  const bool other = mov && (gr.flags & GF_STOPPABLE);
+  double xpc[D];
+  if (act) ldv<D>(P.cur, d, xpc);
+
+  // ---- node-node contact: self-contact first, then grains j ascending (timeloop.h:709-747) ----
+  if ((selfc || other) && p_bdry) {
+    double bmn[D], bmx[D];
+    grain_box<D>(P, g, bmn, bmx);
+    float pf[D];
+    ldf<D>(P.curf, d, pf);
+    int32_t cc[3] = {0, 0, 0};
+    for (int c = 0; c < D; ++c) cc[c] = (int32_t)floorf(pf[c] * in.inv_cell_f);
+    const float thr2 = in.cell_f * in.cell_f;
+    unsigned long long keys[MAX_CAND];
+    uint32_t idx[MAX_CAND];
+    int nc = 0;
+    uint32_t seen[27];
+    int nseen = 0;
+    const int nnb = (D == 2) ? 9 : 27;
+    for (int nb = 0; nb < nnb; ++nb) {
+      int ox = nb % 3 - 1, oy = (nb / 3) % 3 - 1, oz = (D == 3) ? (nb / 9 - 1) : 0;
+      uint32_t m = (D == 2) ? morton2((uint32_t)(cc[0] + ox), (uint32_t)(cc[1] + oy))
+                            : morton3((uint32_t)(cc[0] + ox), (uint32_t)(cc[1] + oy), (uint32_t)(cc[2] + oz));
+      uint32_t bucket = in.table_off + (m & in.table_mask);
+      bool dup = false;
+      for (int s = 0; s < nseen; ++s) dup = dup || (seen[s] == bucket);
+      if (dup) continue;
+      seen[nseen++] = bucket;
+      const uint32_t b0 = P.cell_start[bucket], b1 = P.cell_start[bucket + 1];
+      for (uint32_t b = b0; b < b1; ++b) {
+        const uint32_t q = P.sorted[b];
+        if (q == d) continue;
+        float qf[D];
+        ldf<D>(P.curf, q, qf);
+        float d2 = 0.f;
+        for (int c = 0; c < D; ++c) {
+          float dd = qf[c] - pf[c];
+          d2 += dd * dd;
+        }
+        if (d2 > thr2) continue;
+        const uint32_t gq = P.node_grain[q];
+        const bool same = (gq == g);
+        if (same ? !selfc : !other) continue;
+        if (P.nl_bdry_only && P.bdry_rank[q] == NONE) continue;
+        if (!same) {
+          double qmn[D], qmx[D];
+          grain_box<D>(P, gq, qmn, qmx);
+          if (!boxes_touch<D>(bmn, bmx, qmn, qmx, in.contact_rad)) continue;
+        }
+        const uint32_t sub = P.nl_bdry_only ? P.bdry_rank[q] : (q - P.grain[gq].node_begin);
+        const unsigned long long key =
+            ((unsigned long long)(same ? 0u : 1u) << 63) | ((unsigned long long)gq << 32) | sub;
+        insert_cand<D>(keys, idx, nc, key, q, P);
+      }
+    }
+    const uint32_t mydeg = P.node_deg[d];
+    for (int ci = 0; ci < nc; ++ci) {
+      const uint32_t q = idx[ci];
+      const bool same = (keys[ci] >> 63) == 0;
+      double xq[D], dir[D];
+      ldv<D>(P.cur, q, xq);
+      for (int c = 0; c < D; ++c) dir[c] = xq[c] - xpc[c];
+      double n2 = dir[0] * dir[0];
+      for (int c = 1; c < D; ++c) n2 = n2 + dir[c] * dir[c];
+      const double dn = sqrt(n2);
+      double Rc = in.contact_rad, Kn = in.normal_stiffness;
+      if (same) {
+        bool bonded = false;
+        for (uint32_t k = 0; k < mydeg && !bonded; ++k) {
+          if (((P.alive[w0 + k] >> lane) & 1u) && P.bcol[slot0 + 32u * k] == q) bonded = true;
+        }
+        if (bonded) continue;
+        double pp[D], pq[D], r[D];
+        ldv<D>(P.pos, d, pp);
+        ldv<D>(P.pos, q, pq);
+        for (int c = 0; c < D; ++c) r[c] = pp[c] - pq[c];
+        double r2 = r[0] * r[0];
+        for (int c = 1; c < D; ++c) r2 = r2 + r[c] * r[c];
+        const double ref = sqrt(r2);
+        if (ref < in.contact_rad) {
+          Rc = ref;
+          Kn = gr.cnot / ref;
+        } else {
+          Rc = in.contact_rad;
+          Kn = gr.cnot / in.contact_rad;
+        }
+      }
+      if (!(dn <= Rc)) continue;
+      if (P.record_pairs) {
+        my_pairs += 1;
+        my_hash += splitmix64(((unsigned long long)d << 32) | q);
+      }
+      if (dn == 0.0) my_close += 1;
+      double u[D];
+      for (int c = 0; c < D; ++c) u[c] = dir[c] / dn;
+      const double crc = Rc - dn;
+      const double nvol = P.vol[q];
+      const double s1 = ((-Kn) * crc) * nvol;
+      double fc[D];
+      for (int c = 0; c < D; ++c) fc[c] = s1 * u[c];
+      double cf2 = fc[0] * fc[0];
+      for (int c = 1; c < D; ++c) cf2 = cf2 + fc[c] * fc[c];
+      const double cfn = sqrt(cf2);
+      for (int c = 0; c < D; ++c) f[c] = f[c] + fc[c];
+      if (P.allow_damping || P.allow_friction) {
+        double vq[D], rv[D];
+        ldv<D>(P.vel_in, q, vq);
+        for (int c = 0; c < D; ++c) rv[c] = vp[c] - vq[c];
+        double rvp = rv[0] * u[0];
+        for (int c = 1; c < D; ++c) rvp = rvp + rv[c] * u[c];
+        if (P.allow_damping) {
+          const double dc = ((2.0 * in.damping_ratio) * sqrt(Kn * gr.rho)) * sqrt(nvol);
+          for (int c = 0; c < D; ++c) f[c] = f[c] + ((-dc) * (rvp * u[c]));
+        }
+        if (P.allow_friction) {
+          double tg[D];
+          for (int c = 0; c < D; ++c) tg[c] = rv[c] - (rvp * u[c]);
+          double t2 = tg[0] * tg[0];
+          for (int c = 1; c < D; ++c) t2 = t2 + tg[c] * tg[c];
+          const double tn = sqrt(t2);
+          if (tn > 0) {
+            const double mu = in.friction_coefficient;
+            double sfr = (-mu) * cfn;
+            if (tn < (((mu * cfn) * P.dt) / gr.rho)) sfr = ((-tn) / gr.rho) / P.dt;
+            for (int c = 0; c < D; ++c) f[c] = f[c] + sfr * (tg[c] / tn);
+          }
+        }
+      }
+    }
+  }
+
+  // ---- analytic wall (timeloop.h:753-769 -> contact.h:900-964) ----
+  if (mov && other && p_bdry && in.allow_wall) {
+    double bmn[D], bmx[D];
+    grain_box<D>(P, g, bmn, bmx);
+    if (!within_interior<D>(bmn, bmx, in.wall, in.contact_rad)) {
+      const double vol_i = P.vol[d];
+      constexpr int NS = 2 * D;
+      // (side, dir) in the reference's call order
+      const int order2[4][2] = {{3, 1}, {0, 0}, {1, 0}, {2, 1}};
+      const int order3[6][2] = {{0, 0}, {3, 0}, {1, 1}, {4, 1}, {2, 2}, {5, 2}};
+      for (int k = 0; k < NS; ++k) {
+        const int side = (D == 2) ? order2[k][0] : order3[k][0];
+        const int dir = (D == 2) ? order2[k][1] : order3[k][1];
+        const double dist = xpc[dir] - in.wall[side];
+        const double R = in.contact_rad;
+        if (!(fabs(dist) <= R)) continue;
+        const double dd = fabs(dist);
+        // segment_mass<dim>(R, d) (contact.h:16-41)
+        double Area, I;
+        if constexpr (D == 2) {
+          Area = M_PI * pow(R, 2.0) / 2 - pow(R, 2.0) * asin(dd / R) - sqrt(R * R - dd * dd) * dd;
+          I = 0.0 * pow((R * R - dd * dd), 1.5);  // 2 / 3 is integer division in the reference
+        } else {
+          Area = M_PI / 3 * pow((R - dd), 2.0) * (2 * R - dd);
+          I = M_PI / 4 * pow(pow(R, 2.0) - pow(dd, 2.0), 2.0);
+        }
+        const double centroid = I / Area;
+        const double crc = R - centroid;
+        const double pcrc = crc > 0 ? crc : 0;
+        const double F = (in.normal_stiffness * pcrc) * Area;
+        const double c_sign = dist > 0 ? 1 : -1;
+        f[dir] = f[dir] + (c_sign * F);
+        WallRec rec;
+        rec.a_normal = (vol_i * c_sign) * F;
+        rec.a_t1 = 0;
+        rec.a_t2 = 0;
+        rec.a_damp = 0;
+        rec.gid = d;
+        rec.side = (uint16_t)side;
+        rec.has_fric = 0;
+        rec.has_damp = 0;
+        double rv[D];
+        for (int c = 0; c < D; ++c) rv[c] = vp[c];
+        rv[dir] = rv[dir] - in.wall_speed[side];
+        if (P.allow_friction) {
+          const double mu = in.friction_coefficient;
+          if constexpr (D == 2) {
+            const int tg = (dir + 1) % 2;
+            if (fabs(rv[tg]) > 0) {
+              const double vts = rv[tg] > 0 ? 1 : -1;
+              double ff = ((-mu) * fabs(F)) * vts;
+              if (fabs(rv[tg]) < (((mu * fabs(F)) * P.dt) / gr.rho)) ff = ((-rv[tg]) * gr.rho) / P.dt;
+              f[tg] = f[tg] + ff;
+              rec.a_t1 = vol_i * ff;
+              rec.has_fric = 1;
+            }
+          } else {
+            const int t1 = (dir + 1) % 3, t2 = (dir + 2) % 3;
+            const double v1 = rv[t1], v2 = rv[t2];
+            const double vn = sqrt(pow(v1, 2.0) + pow(v2, 2.0));
+            if (vn > 0) {
+              const double u1 = v1 / vn, u2 = v2 / vn;
+              double ff1 = ((-mu) * fabs(F)) * u1;
+              double ff2 = ((-mu) * fabs(F)) * u2;
+              if (vn < (((mu * fabs(F)) * P.dt) / gr.rho)) {
+                ff1 = (((-vn) / gr.rho) / P.dt) * u1;
+                ff2 = (((-vn) / gr.rho) / P.dt) * u2;
+              }
+              f[t1] = f[t1] + ff1;
+              f[t2] = f[t2] + ff2;
+              rec.a_t1 = vol_i * ff1;
+              rec.a_t2 = vol_i * ff2;
+              rec.has_fric = 1;
+            }
+          }
+        }
+        if (P.allow_damping) {
+          const double dc = ((2.0 * in.damping_ratio) * sqrt(in.normal_stiffness * gr.rho)) * sqrt(fabs(Area));
+          const double df = (-dc) * rv[dir];
+          f[dir] = f[dir] + df;
+          rec.a_damp = vol_i * df;
+          rec.has_damp = 1;
+        }
+        const uint32_t slot = atomicAdd(P.wrec_count, 1u);
+        if (slot < P.wrec_cap) {
+          P.wrec[slot] = rec;
+        } else {
+          set_status(P.status, PG_ECAPACITY);
+        }
+      }
+    }
+  }
+
+  // ---- external force and torque (timeloop.h:774-824) ----
+  if (mov) {
+    double ef[D];
+    ldv<D>(P.extf, d, ef);
+    if (P.gradient_extforce) {
+      double sc = (double)t / (double)P.extforce_maxstep;
+      if (sc > 1) sc = 1;
+      for (int c = 0; c < D; ++c) f[c] = f[c] + sc * ef[c];
+    } else {
+      for (int c = 0; c < D; ++c) f[c] = f[c] + ef[c];
+    }
+    if (P.enable_torque) {
+      const uint32_t ta = gr.torque_axis;
+      double r[3] = {0, 0, 0}, rp[3] = {0, 0, 0};
+      for (int c = 0; c < D; ++c) r[c] = xpc[c] - P.torque_c[(size_t)g * 3 + c];
+      if (D == 3) r[ta] = 0;
+      if (D == 3) rp[ta] = 0;
+      rp[(ta + 1) % 3] = -r[(ta + 2) % 3];
+      rp[(ta + 2) % 3] = r[(ta + 1) % 3];
+      double pn2 = rp[0] * rp[0];
+      for (int c = 1; c < D; ++c) pn2 = pn2 + rp[c] * rp[c];
+      const double pn = sqrt(pn2);
+      if (pn > 0) {
+        for (int c = 0; c < D; ++c) rp[c] = rp[c] / pn;
+      } else {
+        rp[(ta + 1) % 3] = 0;
+        rp[(ta + 2) % 3] = 0;
+      }
+      for (int c = 0; c < D; ++c) f[c] = f[c] + (gr.torque_val * rp[c]);
+    }
+  }
+
+  // ---- velocity update (timeloop.h:834-863) ----
+  if (act) {
+    if (mov) {
+      double ao[D], a[D], v[D];
+      ldv<D>(P.acc, d, ao);
+      for (int c = 0; c < D; ++c) {
+        a[c] = gr.one_over_rho * f[c];
+        double tmp = ao[c] + a[c];
+        tmp = tmp * P.half_dt;
+        v[c] = vp[c] + tmp;
+      }
+      if (P.clamped[d]) {
+        for (int c = 0; c < D; ++c) {
+          a[c] = 0.0;
+          v[c] = 0.0;
+        }
+        P.clamp_pending[d] = 1;
+      }
+      stv<D>(P.acc, d, a);
+      stv<D>(P.vel_out, d, v);
+    } else {
+      stv<D>(P.vel_out, d, vp);
+    }
+    stv<D>(P.force, d, f);  // zero for grains that are not movable
+  }
+
+  // ---- diagnostics: warp-aggregated counters ----
+  if (P.record_pairs) {
+    for (int off = 16; off > 0; off >>= 1) {
+      my_pairs += __shfl_down_sync(0xffffffffu, my_pairs, off);
+      my_hash += __shfl_down_sync(0xffffffffu, my_hash, off);
+    }
+    if (lane == 0 && my_pairs) {
+      atomicAdd(&P.pair_acc[0], my_pairs);
+      atomicAdd(&P.pair_acc[1], my_hash);
+    }
+  }
+  if (my_close) atomicAdd(P.too_close, my_close);
+}
+
+// ---------------------------------------------------------------------------------------------
+// k_finalize: one block. Wall reactions in node order, pair log, wall move, step counter.
+// ---------------------------------------------------------------------------------------------
+template <int D>
+__global__ void __launch_bounds__(FINAL_THREADS) k_finalize(const Dev P) {
+  extern __shared__ unsigned long long skey[];
+  constexpr int NS = 2 * D;
+  const uint32_t tid = threadIdx.x;
+  const uint32_t t = *P.step;
+  const uint32_t R = *P.wrec_count;
+  const uint32_t nrx = P.I * NS * D;
+  for (uint32_t i = tid; i < nrx; i += blockDim.x) P.reaction[i] = 0.0;
+  if (R > 0) {
+    if (R > (uint32_t)WREC_SMEM_CAP || R > P.wrec_cap) {
+      if (tid == 0) set_status(P.status, PG_ECAPACITY);
+    } else {
+      uint32_t n2 = 32;
+      while (n2 < R) n2 <<= 1;
+      for (uint32_t i = tid; i < n2; i += blockDim.x) {
+        if (i < R) {
+          const WallRec& r = P.wrec[i];
+          skey[i] = ((unsigned long long)r.gid << 32) | ((unsigned long long)r.side << 28) | i;
+        } else {
+          skey[i] = ~0ull;
+        }
+      }
+      __syncthreads();
+      for (uint32_t k = 2; k <= n2; k <<= 1) {
+        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+          for (uint32_t i = tid; i < n2; i += blockDim.x) {
+            uint32_t l = i ^ j;
+            if (l > i) {
+              unsigned long long a = skey[i], b = skey[l];
+              bool up = ((i & k) == 0);
+              if ((a > b) == up) {
+                skey[i] = b;
+                skey[l] = a;
+              }
+            }
+          }
+          __syncthreads();
+        }
+      }
+      for (uint32_t p = tid; p < P.I * NS; p += blockDim.x) {
+        const uint32_t inst = p / NS, side = p % NS;
+        const unsigned long long lo_key = (unsigned long long)P.inst[inst].node_begin << 32;
+        const unsigned long long hi_key = (unsigned long long)P.inst[inst].node_end << 32;
+        uint32_t lo = 0, hi = R;
+        while (lo < hi) {
+          uint32_t mid = (lo + hi) >> 1;
+          if (skey[mid] < lo_key) lo = mid + 1; else hi = mid;
+        }
+        double r[3] = {0.0, 0.0, 0.0};
+        bool any = false;
+        for (uint32_t k = lo; k < R && skey[k] < hi_key; ++k) {
+          if (((skey[k] >> 28) & 0xfu) != side) continue;
+          const WallRec& w = P.wrec[skey[k] & 0x0fffffffu];
+          const int dir = (D == 2) ? ((side == 0 || side == 1) ? 0 : 1) : (int)(side % 3);
+          r[dir] = r[dir] - w.a_normal;
+          if (w.has_fric) {
+            if constexpr (D == 2) {
+              const int tg = (dir + 1) % 2;
+              r[tg] = r[tg] - w.a_t1;
+            } else {
+              r[(dir + 1) % 3] = r[(dir + 1) % 3] - w.a_t1;
+              r[(dir + 2) % 3] = r[(dir + 2) % 3] - w.a_t2;
+            }
+          }
+          if (w.has_damp) r[dir] = r[dir] - w.a_damp;
+          any = true;
+        }
+        if (any) {
+          for (int c = 0; c < D; ++c) P.reaction[((size_t)inst * NS + side) * D + c] = r[c];
+        }
+      }
+    }
+  }
+  __syncthreads();
+  if (tid == 0) {
+    if (P.record_pairs) {
+      const uint32_t slot = (t - 1) % P.log_cap;
+      P.log_count[slot] = P.pair_acc[0];
+      P.log_hash[slot] = P.pair_acc[1];
+      P.pair_acc[0] = 0;
+      P.pair_acc[1] = 0;
+    }
+    *P.wrec_count = 0;
+    *P.step = t + 1;
+  }
+  for (uint32_t p = tid; p < P.I * NS; p += blockDim.x) {
+    InstDev* in = &P.inst[p / NS];
+    const int s = p % NS;
+    in->wall[s] = in->wall[s] + in->wall_speed[s] * P.dt;
+  }
+  for (uint32_t i = tid; i < P.G * NS; i += blockDim.x) {
+    P.bbox[i] = ((i % NS) < (uint32_t)D) ? ~0ull : 0ull;
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// host-side launchers
+// ---------------------------------------------------------------------------------------------
+static inline uint32_t cdiv(uint32_t a, uint32_t b) { return (a + b - 1) / b; }
+
+template <int D>
+static void launch_step_t(const Dev& P, const LaunchCfg& L, cudaStream_t s, uint64_t* launches,
+                          cudaEvent_t e0 = nullptr, cudaEvent_t e1 = nullptr) {
+  const uint32_t nthr_nodes = P.n_chunks * 32;
+  k_predict<D><<<cdiv(P.N, 256), 256, 0, s>>>(P);
+  const uint32_t ntiles = cdiv(P.table_total, SCAN_TILE);
+  k_scan_reduce<<<ntiles, SCAN_THREADS, 0, s>>>(P);
+  k_scan_final<<<ntiles, SCAN_THREADS, 0, s>>>(P);
+  k_scatter<<<cdiv(P.N, 256), 256, 0, s>>>(P);
+  *launches += 4;
+  if (P.enable_torque) {
+    k_torque_center<D><<<cdiv(P.G, 128), 128, 0, s>>>(P);
+    *launches += 1;
+  }
+  if (e0) cudaEventRecord(e0, s);
+  k_force<D><<<cdiv(nthr_nodes, L.force_block), L.force_block, 0, s>>>(P);
+  if (e1) cudaEventRecord(e1, s);
+  k_finalize<D><<<1, FINAL_THREADS, WREC_SMEM_CAP * sizeof(unsigned long long), s>>>(P);
+  *launches += 2;
+}
+
+cudaError_t kernels_init() {
+  cudaError_t e = cudaFuncSetAttribute(k_finalize<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       WREC_SMEM_CAP * (int)sizeof(unsigned long long));
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_finalize<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              WREC_SMEM_CAP * (int)sizeof(unsigned long long));
+}
+
+void launch_step(const Dev& P, const LaunchCfg& L, cudaStream_t s, uint64_t* launches) {
+  if (P.dim == 2) {
+    launch_step_t<2>(P, L, s, launches);
+  } else {
+    launch_step_t<3>(P, L, s, launches);
+  }
+}
+
+void launch_step_timed(const Dev& P, const LaunchCfg& L, cudaStream_t s, uint64_t* launches,
+                       cudaEvent_t e0, cudaEvent_t e1) {
+  if (P.dim == 2) {
+    launch_step_t<2>(P, L, s, launches, e0, e1);
+  } else {
+    launch_step_t<3>(P, L, s, launches, e0, e1);
+  }
+}
+
+const void* force_kernel_ptr(uint32_t dim) {
+  return dim == 2 ? (const void*)k_force<2> : (const void*)k_force<3>;
+}
+
+}  // namespace pg

@@ -1,0 +1,23 @@
+// Host-side entry points of the device kernels (pg_kernels.cu, pg_kernels_mixed.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "pg_device.cuh"
+
+namespace pg {
+
+struct LaunchCfg {
+  uint32_t force_block = 128;
+};
+
+cudaError_t kernels_init();
+// Enqueue one FP64 time step on stream s. Adds the number of kernel launches to *launches.
+void launch_step(const Dev& P, const LaunchCfg& L, cudaStream_t s, uint64_t* launches);
+// Same as launch_step, with CUDA events e0/e1 recorded around the fused force kernel.
+void launch_step_timed(const Dev& P, const LaunchCfg& L, cudaStream_t s, uint64_t* launches,
+                       cudaEvent_t e0, cudaEvent_t e1);
+const void* force_kernel_ptr(uint32_t dim);
+
+}  // namespace pg

@@ -1,0 +1,148 @@
+"""Python face of the GPU engine (C ABI in include/perigrain.h).
+
+:class:`Simulation` mirrors the reference's in-process entry point
+``run_timeloop<dim>(PArr, Timeloop, Contact, RectWall)`` (src/particle/timeloop.h:501-1015):
+it owns the grains of one or more independent simulations on the GPU and advances them by
+time steps; fields come back in the reference's node order. :func:`run_simulation` is the whole
+``bin/simulate2d`` / ``bin/simulate3d`` process contract (config/main.conf + data/hdf5/all.h5 in,
+output/hdf5/*.h5 out).
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _native as N
+
+
+class Simulation:
+    def __init__(self, setup, dt, enable_fracture=1, nl_bdry_only=0, allow_damping=1, allow_friction=1,
+                 self_contact=1, enable_torque=0, gradient_extforce=0, extforce_maxstep=0, precision="fp64",
+                 record_pairs=False, pair_log_capacity=1024, first_step=1, max_contacts=48, block_size=0):
+        L = N.lib()
+        self.setup = setup
+        self.dim = setup.dim
+        cfg = N.Config()
+        L.pg_config_default(C.byref(cfg))
+        cfg.dt = dt
+        cfg.enable_fracture = int(enable_fracture)
+        cfg.nl_bdry_only = int(nl_bdry_only)
+        cfg.allow_damping = int(allow_damping)
+        cfg.allow_friction = int(allow_friction)
+        cfg.self_contact = int(self_contact)
+        cfg.enable_torque = int(enable_torque)
+        cfg.gradient_extforce = int(gradient_extforce)
+        cfg.extforce_maxstep = int(extforce_maxstep)
+        cfg.precision = N.PG_MIXED if precision == "mixed" else N.PG_FP64
+        cfg.record_pairs = int(bool(record_pairs))
+        cfg.pair_log_capacity = int(pair_log_capacity)
+        cfg.first_step = int(first_step)
+        cfg.max_contacts = int(max_contacts)
+        cfg.block_size = int(block_size)
+        self.cfg = cfg
+        self._desc = setup.desc()
+        h = C.c_void_p()
+        N.check(L.pg_create(C.byref(self._desc), C.byref(cfg), C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            N.lib().pg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def step(self, n=1):
+        N.check(N.lib().pg_step(self.h, int(n)))
+
+    def synchronize(self):
+        N.check(N.lib().pg_synchronize(self.h))
+
+    def next_step(self):
+        t = C.c_uint64()
+        N.check(N.lib().pg_get_step(self.h, C.byref(t)))
+        return t.value
+
+    def field(self, name):
+        out = np.empty((self.setup.n_nodes, self.dim), np.float64)
+        N.check(N.lib().pg_get_field(self.h, N.FIELD[name], N.ptr(out, C.c_double)))
+        return out
+
+    def set_field(self, name, a):
+        a = np.ascontiguousarray(a, np.float64).reshape(self.setup.n_nodes, self.dim)
+        N.check(N.lib().pg_set_field(self.h, N.FIELD[name], N.ptr(a, C.c_double)))
+
+    def bond_alive(self):
+        out = np.empty(max(1, self.setup.n_bonds), np.uint8)
+        N.check(N.lib().pg_get_bond_alive(self.h, N.ptr(out, C.c_uint8)))
+        return out[: self.setup.n_bonds]
+
+    def set_bond_alive(self, a):
+        a = np.ascontiguousarray(a, np.uint8)
+        N.check(N.lib().pg_set_bond_alive(self.h, N.ptr(a, C.c_uint8)))
+
+    def break_step(self):
+        out = np.empty(max(1, self.setup.n_bonds), np.uint32)
+        N.check(N.lib().pg_get_bond_break_step(self.h, N.ptr(out, C.c_uint32)))
+        return out[: self.setup.n_bonds]
+
+    def reaction(self):
+        ns = 2 * self.dim
+        out = np.empty((self.setup.n_instances, ns, self.dim), np.float64)
+        N.check(N.lib().pg_get_reaction(self.h, N.ptr(out, C.c_double)))
+        return out
+
+    def wall(self):
+        out = np.empty((self.setup.n_instances, 2 * self.dim), np.float64)
+        N.check(N.lib().pg_get_wall(self.h, N.ptr(out, C.c_double)))
+        return out
+
+    def set_grain_flags(self, grain, movable=-1, stoppable=-1):
+        N.check(N.lib().pg_set_grain_flags(self.h, int(grain), int(movable), int(stoppable)))
+
+    def pair_log(self, n):
+        c = np.empty(n, np.uint64)
+        hs = np.empty(n, np.uint64)
+        N.check(N.lib().pg_get_pair_log(self.h, int(n), N.ptr(c, C.c_uint64), N.ptr(hs, C.c_uint64)))
+        return c, hs
+
+    def device_status(self):
+        st = C.c_int32()
+        tc = C.c_uint64()
+        N.check(N.lib().pg_get_device_status(self.h, C.byref(st), C.byref(tc)))
+        return st.value, tc.value
+
+    def launch_count(self):
+        n = C.c_uint64()
+        N.check(N.lib().pg_get_launch_count(self.h, C.byref(n)))
+        return n.value
+
+    def set_timing(self, on):
+        N.check(N.lib().pg_set_timing(self.h, int(bool(on))))
+
+    def kernel_times(self):
+        f, t, n = C.c_double(), C.c_double(), C.c_uint64()
+        N.check(N.lib().pg_get_kernel_times(self.h, C.byref(f), C.byref(t), C.byref(n)))
+        return f.value, t.value, n.value
+
+
+def run_simulation(root=".", dim=2, precision="fp64"):
+    """bin/simulate{2,3}d in-process: reads <root>/config/main.conf and <root>/data/hdf5/all.h5,
+    writes <root>/output/hdf5/."""
+    p = N.PG_MIXED if precision == "mixed" else N.PG_FP64
+    N.check(N.lib().pg_run_simulation(str(root).encode(), int(dim), p))
+
+
+def device_count():
+    n = C.c_int32()
+    rc = N.lib().pg_device_count(C.byref(n))
+    return n.value if rc == N.PG_OK else 0
