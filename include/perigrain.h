@@ -125,6 +125,9 @@ const char* pg_status_string(int status);
 const char* pg_last_error(void);
 void pg_config_default(pg_config* cfg);
 
+/* Make `device` the current CUDA device of the calling thread for subsequent pg_create calls
+ * (one process per GPU under torchrun: device = LOCAL_RANK). */
+int pg_select_device(int device);
 /* Copy the setup to the current CUDA device and build the device layout. */
 int pg_create(const pg_setup_desc* setup, const pg_config* cfg, pg_handle** out);
 int pg_destroy(pg_handle* h);
@@ -132,6 +135,9 @@ int pg_destroy(pg_handle* h);
 /* ---- stepping (timeloop.h:608-879: position update, force loop, velocity update, wall move) */
 int pg_step(pg_handle* h, uint32_t nsteps);
 int pg_synchronize(pg_handle* h);
+/* pg_step bracketed by CUDA events on the handle's stream; *elapsed_ms = device time of the
+ * nsteps steps (synchronizes). */
+int pg_step_timed(pg_handle* h, uint32_t nsteps, double* elapsed_ms);
 /* Index t of the next step to be taken. */
 int pg_get_step(pg_handle* h, uint64_t* next_t);
 

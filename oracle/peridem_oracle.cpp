@@ -19,6 +19,8 @@
 // ascending, nodes in loop order); pairs farther apart than the contact radius contribute
 // nothing in the reference, so the result is identical. This is checked bit-for-bit against the
 // reference compiled unmodified (oracle/Makefile, tests/test_oracle_vs_reference.py).
+#include <omp.h>
+
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
@@ -76,6 +78,11 @@ struct orc_sim {
   std::vector<uint32_t> break_step;
   std::vector<uint64_t> log_count, log_hash;
   uint64_t too_close = 0;
+  // reference_structured: enumerate node pairs the way the reference does (all n_i x n_j pairs
+  // of bbox-touching grains, std::find before the distance test, bounding boxes recomputed per
+  // grain pair, the two grains copied per contact call) -- same arithmetic, the reference's cost.
+  int reference_structured = 0;
+  int threads = 1;
 
   double& v(std::vector<double>& a, uint32_t i, uint32_t c) { return a[(size_t)i * D + c]; }
 
@@ -197,7 +204,10 @@ struct orc_sim {
     if (!(do_compute && (dn <= Rc))) return;
     *pc += 1;
     *ph += splitmix64(((uint64_t)(C.gid0 + i) << 32) | (uint64_t)(Nn.gid0 + j));
-    if (dn == 0) ++too_close;
+    if (dn == 0) {
+#pragma omp atomic
+      ++too_close;
+    }
     double u[3], fc[3];
     for (uint32_t c = 0; c < D; ++c) u[c] = dir[c] / dn;
     double crc = (Rc - dn);
@@ -304,24 +314,44 @@ struct orc_sim {
     }
   };
 
-  void step() {
-    const double dt = cfg.dt;
-    for (auto& in : I)
-      for (auto& r : in.reaction)
-        for (double& x : r) x = 0.0;
-    // loop 1: position update
-    for (auto& g : G) {
-      for (uint32_t i = 0; i < g.n; ++i)
-        for (uint32_t c = 0; c < D; ++c) {
-          if (g.movable) g.disp[i * D + c] += dt * g.vel[i * D + c] + (dt * dt * 0.5) * g.acc[i * D + c];
-          g.cur[i * D + c] = g.pos[i * D + c] + g.disp[i * D + c];
-        }
+  // The reference's loop structure (timeloop.h:709-747 -> contact.h:668-812): self-contact over
+  // all node pairs of grain i, then every other grain j whose extended bounding box (recomputed
+  // for each pair, timeloop.h:723-730) touches, over all node pairs; each call works on copies
+  // of both grains (contact.h:669 passes ParticleN by value).
+  void contact_reference_structured(Inst& in, uint32_t gi, bool self, std::vector<double>& ft, uint64_t* pc,
+                                    uint64_t* ph) {
+    Grain& g = G[gi];
+    auto loop_list = [&](const Grain& h) {
+      std::vector<uint32_t> l;
+      if (cfg.nl_bdry_only) return h.bdry;
+      for (uint32_t i = 0; i < h.n; ++i) l.push_back(i);
+      return l;
+    };
+    auto visit = [&](Grain& C, Grain& Nn, bool is_self) {
+      std::vector<uint32_t> li = loop_list(C), lj = loop_list(Nn);
+      for (uint32_t i : li)
+        for (uint32_t j : lj) pair(C, i, Nn, j, is_self, in, &ft[i * D], pc, ph);
+    };
+    if (self && cfg.self_contact) {
+      Grain c1 = g, c2 = g;
+      visit(c1, c2, true);
     }
-    std::vector<std::vector<double>> boxes(G.size());
-    for (size_t k = 0; k < G.size(); ++k) boxes[k] = minmax(G[k]);
+    if (g.stoppable) {
+      std::vector<double> C = minmax(g);
+      for (uint32_t gj = in.g0; gj < in.g1; ++gj) {
+        if (gj == gi) continue;
+        std::vector<double> Nb = minmax(G[gj]);
+        if (intersects(C, Nb, in.Rc)) {
+          Grain c1 = g, c2 = G[gj];
+          visit(c1, c2, false);
+        }
+      }
+    }
+  }
+
+  void force_instance(Inst& in, const std::vector<std::vector<double>>& boxes, uint64_t* pcp, uint64_t* php) {
     uint64_t pc = 0, ph = 0;
-    // loop 2, one instance at a time (instances never interact)
-    for (auto& in : I) {
+    {
       // cell grid of this instance
       const double cell = in.Rc > 0 ? in.Rc * 1.01 : 1.0;
       std::unordered_map<CellKey, std::vector<std::pair<uint32_t, uint32_t>>, CellHash> grid;
@@ -341,6 +371,9 @@ struct orc_sim {
           bond_force(g, ft);
           const bool self = cfg.enable_fracture && g.breakable;
           if (self) remove_bonds(g);
+          if (reference_structured) {
+            contact_reference_structured(in, gi, self, ft, &pc, &ph);
+          } else
           // candidate lists per node: (order key, grain, node)
           for (uint32_t i = 0; i < g.n; ++i) {
             if (cfg.nl_bdry_only && g.loop_pos[i] == UINT32_MAX) continue;
@@ -436,6 +469,33 @@ struct orc_sim {
         }
         g.force = ft;
       }
+    }
+    *pcp += pc;
+    *php += ph;
+  }
+
+  void step() {
+    const double dt = cfg.dt;
+    for (auto& in : I)
+      for (auto& r : in.reaction)
+        for (double& x : r) x = 0.0;
+    // loop 1: position update
+    for (auto& g : G) {
+      for (uint32_t i = 0; i < g.n; ++i)
+        for (uint32_t c = 0; c < D; ++c) {
+          if (g.movable) g.disp[i * D + c] += dt * g.vel[i * D + c] + (dt * dt * 0.5) * g.acc[i * D + c];
+          g.cur[i * D + c] = g.pos[i * D + c] + g.disp[i * D + c];
+        }
+    }
+    std::vector<std::vector<double>> boxes(G.size());
+    for (size_t k = 0; k < G.size(); ++k) boxes[k] = minmax(G[k]);
+    uint64_t pc = 0, ph = 0;
+    // loop 2, one instance at a time (instances never interact)
+    if (threads > 1) {
+#pragma omp parallel for schedule(dynamic) num_threads(threads) reduction(+ : pc, ph)
+      for (size_t k = 0; k < I.size(); ++k) force_instance(I[k], boxes, &pc, &ph);
+    } else {
+      for (auto& in : I) force_instance(in, boxes, &pc, &ph);
     }
     log_count.push_back(pc);
     log_hash.push_back(ph);
@@ -646,5 +706,13 @@ int orc_get_pair_log(orc_sim* o, uint64_t* count, uint64_t* hash) {
 }
 
 uint64_t orc_too_close(orc_sim* o) { return o->too_close; }
+
+// reference_structured: 1 = enumerate pairs with the reference's loops (its cost model);
+// threads > 1 = run independent instances concurrently (OpenMP).
+int orc_set_mode(orc_sim* o, int reference_structured, int threads) {
+  o->reference_structured = reference_structured;
+  o->threads = threads < 1 ? 1 : threads;
+  return PG_OK;
+}
 
 }  // extern "C"

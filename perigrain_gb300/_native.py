@@ -78,10 +78,12 @@ PROTOTYPES = [
     ("pg_status_string", C.c_char_p, [C.c_int]),
     ("pg_last_error", C.c_char_p, []),
     ("pg_config_default", None, [C.POINTER(Config)]),
+    ("pg_select_device", C.c_int, [C.c_int]),
     ("pg_create", C.c_int, [C.POINTER(SetupDesc), C.POINTER(Config), C.POINTER(C.c_void_p)]),
     ("pg_destroy", C.c_int, [C.c_void_p]),
     ("pg_step", C.c_int, [C.c_void_p, C.c_uint32]),
     ("pg_synchronize", C.c_int, [C.c_void_p]),
+    ("pg_step_timed", C.c_int, [C.c_void_p, C.c_uint32, f64p]),
     ("pg_get_step", C.c_int, [C.c_void_p, u64p]),
     ("pg_get_field", C.c_int, [C.c_void_p, C.c_int, f64p]),
     ("pg_set_field", C.c_int, [C.c_void_p, C.c_int, f64p]),

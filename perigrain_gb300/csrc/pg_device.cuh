@@ -111,6 +111,11 @@ struct Dev {
   int32_t enable_torque, gradient_extforce, record_pairs;
   uint32_t extforce_maxstep;
   uint32_t max_cand;
+  // mixed precision (PG_MIXED): FP32 hi/lo pairs (hi = (float)x, lo = (float)(x - hi)) of the FP64
+  // displacement, of the bond reference positions and of CurrPos (both relative to the instance
+  // origin), 2*SF floats per node; FP32 acceleration, force, external force and volume.
+  float *disp_hl, *xpos_hl, *cur_hl;
+  float *acc_f, *force_f, *extf_f, *vol_f;
 };
 
 __host__ __device__ inline unsigned long long dbl_to_ordered(double x) {

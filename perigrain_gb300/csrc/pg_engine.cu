@@ -13,6 +13,7 @@
 
 #include "pg_device.cuh"
 #include "pg_kernels.h"
+#include "pg_kernels_mixed.h"
 
 using namespace pg;
 
@@ -91,7 +92,11 @@ static void set_vel(pg_handle* h, Dev& P, int parity) {
 static void enqueue_step(pg_handle* h, int parity, uint64_t* launches) {
   Dev P = h->P;
   set_vel(h, P, parity);
-  launch_step(P, h->L, h->stream, launches);
+  if (h->precision == PG_MIXED) {
+    launch_step_mixed(P, h->L, h->stream, launches);
+  } else {
+    launch_step(P, h->L, h->stream, launches);
+  }
 }
 
 static int build_graphs(pg_handle* h) {
@@ -114,6 +119,62 @@ static int build_graphs(pg_handle* h) {
     CU(e);
     h->graph_launches_per = n;
   }
+  return PG_OK;
+}
+
+// hi/lo FP32 image of FP64 vectors (hi = (float)x, lo = (float)(x - hi)), layout of ld_hl():
+// 2D [hx, hy, lx, ly]; 3D [hx, hy, hz, 0, lx, ly, lz, 0]
+static void pack_hl(const double* x, uint32_t N, uint32_t D, const std::vector<double>* origin_of_node,
+                    std::vector<float>* out) {
+  const uint32_t SF = (D == 2) ? 2 : 4;
+  out->assign((size_t)N * 2 * SF, 0.f);
+  for (uint32_t i = 0; i < N; ++i)
+    for (uint32_t c = 0; c < D; ++c) {
+      double v = x[(size_t)i * D + c] - (origin_of_node ? (*origin_of_node)[(size_t)i * 3 + c] : 0.0);
+      float hi = (float)v;
+      float lo = (float)(v - (double)hi);
+      (*out)[(size_t)i * 2 * SF + c] = hi;
+      (*out)[(size_t)i * 2 * SF + SF + c] = lo;
+    }
+}
+
+static void pack_f(const double* x, uint32_t N, uint32_t D, std::vector<float>* out) {
+  const uint32_t SF = (D == 2) ? 2 : 4;
+  out->assign((size_t)N * SF, 0.f);
+  for (uint32_t i = 0; i < N; ++i)
+    for (uint32_t c = 0; c < D; ++c) (*out)[(size_t)i * SF + c] = (float)x[(size_t)i * D + c];
+}
+
+static int mixed_setup(pg_handle* h, const pg_setup_desc* s) {
+  Dev& P = h->P;
+  const uint32_t N = P.N, D = h->dim, SF = (D == 2) ? 2 : 4;
+  CU(h->dalloc(&P.disp_hl, (size_t)N * 2 * SF));
+  CU(h->dalloc(&P.xpos_hl, (size_t)N * 2 * SF));
+  CU(h->dalloc(&P.cur_hl, (size_t)N * 2 * SF));
+  CU(h->dalloc(&P.acc_f, (size_t)N * SF));
+  CU(h->dalloc(&P.force_f, (size_t)N * SF));
+  CU(h->dalloc(&P.extf_f, (size_t)N * SF));
+  CU(h->dalloc(&P.vol_f, N));
+  std::vector<double> org((size_t)N * 3, 0.0);
+  for (uint32_t g = 0; g < P.G; ++g) {
+    const InstDev& in = h->inst_host[s->grain_instance[g]];
+    for (uint32_t i = s->grain_node_offset[g]; i < s->grain_node_offset[g + 1]; ++i)
+      for (uint32_t c = 0; c < 3; ++c) org[(size_t)i * 3 + c] = in.origin[c];
+  }
+  std::vector<float> tmp;
+  pack_hl(s->pos, N, D, &org, &tmp);
+  CU(cudaMemcpy(P.xpos_hl, tmp.data(), tmp.size() * 4, cudaMemcpyHostToDevice));
+  CU(cudaMemset(P.cur_hl, 0, tmp.size() * 4));
+  pack_hl(s->disp, N, D, nullptr, &tmp);
+  CU(cudaMemcpy(P.disp_hl, tmp.data(), tmp.size() * 4, cudaMemcpyHostToDevice));
+  pack_f(s->acc, N, D, &tmp);
+  CU(cudaMemcpy(P.acc_f, tmp.data(), tmp.size() * 4, cudaMemcpyHostToDevice));
+  pack_f(s->extforce, N, D, &tmp);
+  CU(cudaMemcpy(P.extf_f, tmp.data(), tmp.size() * 4, cudaMemcpyHostToDevice));
+  CU(cudaMemset(P.force_f, 0, (size_t)N * SF * 4));
+  std::vector<float> v(N);
+  for (uint32_t i = 0; i < N; ++i) v[i] = (float)s->vol[i];
+  CU(cudaMemcpy(P.vol_f, v.data(), (size_t)N * 4, cudaMemcpyHostToDevice));
   return PG_OK;
 }
 
@@ -148,6 +209,11 @@ int pg_device_count(int* count) {
     return fail(PG_ENODEV, cudaGetErrorString(e));
   }
   *count = n;
+  return PG_OK;
+}
+
+int pg_select_device(int device) {
+  CU(cudaSetDevice(device));
   return PG_OK;
 }
 
@@ -205,7 +271,7 @@ static int validate(const pg_setup_desc* s, const pg_config* c) {
       if (s->clamped_nodes[k] >= n1 - n0) return fail(PG_EINVAL, "clamped node out of range");
   }
   if (!(c->dt > 0)) return fail(PG_EINVAL, "dt must be positive");
-  if (c->precision != PG_FP64) return fail(PG_EINVAL, "only PG_FP64 is available in this build");
+  if (c->precision != PG_FP64 && c->precision != PG_MIXED) return fail(PG_EINVAL, "bad precision");
   return PG_OK;
 }
 
@@ -229,6 +295,7 @@ int pg_create(const pg_setup_desc* s, const pg_config* cfg_in, pg_handle** out) 
   if (cfg.first_step == 0) cfg.first_step = 1;
 
   CU(kernels_init());
+  CU(kernels_mixed_init());
 
   std::unique_ptr<pg_handle> h(new pg_handle);
   CU(cudaGetDevice(&h->device));
@@ -238,7 +305,7 @@ int pg_create(const pg_setup_desc* s, const pg_config* cfg_in, pg_handle** out) 
   h->S = S;
   h->precision = cfg.precision;
   h->next_t = cfg.first_step;
-  if (cfg.block_size) h->L.force_block = std::max(32u, (cfg.block_size / 32) * 32);
+  if (cfg.block_size) h->L.force_block = std::min(128u, std::max(32u, (cfg.block_size / 32) * 32));
   Dev& P = h->P;
   P.dim = D;
   P.N = N;
@@ -495,6 +562,10 @@ int pg_create(const pg_setup_desc* s, const pg_config* cfg_in, pg_handle** out) 
   CU(cudaMemset(P.status, 0, 4));
   CU(h->dalloc(&P.too_close, 1));
   CU(cudaMemset(P.too_close, 0, 8));
+  if (h->precision == PG_MIXED) {
+    rc = mixed_setup(h.get(), s);
+    if (rc) return rc;
+  }
   CU(cudaEventCreate(&h->ev_t0));
   CU(cudaEventCreate(&h->ev_t1));
   CU(cudaDeviceSynchronize());
@@ -538,7 +609,11 @@ int pg_step(pg_handle* h, uint32_t nsteps) {
     for (uint32_t k = 0; k < nsteps; ++k) {
       Dev P = h->P;
       set_vel(h, P, h->vel_parity);
-      launch_step_timed(P, h->L, h->stream, &launches, h->ev[2 * k], h->ev[2 * k + 1]);
+      if (h->precision == PG_MIXED) {
+        launch_step_mixed(P, h->L, h->stream, &launches, h->ev[2 * k], h->ev[2 * k + 1]);
+      } else {
+        launch_step_timed(P, h->L, h->stream, &launches, h->ev[2 * k], h->ev[2 * k + 1]);
+      }
       h->vel_parity ^= 1;
     }
     CU(cudaEventRecord(h->ev_t1, h->stream));
@@ -572,6 +647,19 @@ int pg_step(pg_handle* h, uint32_t nsteps) {
   return PG_OK;
 }
 
+int pg_step_timed(pg_handle* h, uint32_t nsteps, double* elapsed_ms) {
+  if (!h || !elapsed_ms) return fail(PG_EINVAL, "null argument");
+  CU(cudaEventRecord(h->ev_t0, h->stream));
+  int rc = pg_step(h, nsteps);
+  if (rc) return rc;
+  CU(cudaEventRecord(h->ev_t1, h->stream));
+  CU(cudaEventSynchronize(h->ev_t1));
+  float ms = 0;
+  CU(cudaEventElapsedTime(&ms, h->ev_t0, h->ev_t1));
+  *elapsed_ms = ms;
+  return check_device_status(h);
+}
+
 int pg_synchronize(pg_handle* h) {
   if (!h) return fail(PG_EINVAL, "null handle");
   CU(cudaStreamSynchronize(h->stream));
@@ -603,6 +691,14 @@ int pg_get_field(pg_handle* h, int field, double* out) {
   int rc = pg_synchronize(h);
   if (rc) return rc;
   const uint32_t N = h->P.N, D = h->dim, S = h->S;
+  if (h->precision == PG_MIXED && (field == PG_FIELD_ACC || field == PG_FIELD_FORCE)) {
+    std::vector<float> tf((size_t)N * S);
+    CU(cudaMemcpy(tf.data(), field == PG_FIELD_ACC ? h->P.acc_f : h->P.force_f, tf.size() * 4,
+                  cudaMemcpyDeviceToHost));
+    for (uint32_t i = 0; i < N; ++i)
+      for (uint32_t c = 0; c < D; ++c) out[(size_t)i * D + c] = (double)tf[(size_t)i * S + c];
+    return PG_OK;
+  }
   std::vector<double> tmp((size_t)N * S);
   CU(cudaMemcpy(tmp.data(), src, tmp.size() * 8, cudaMemcpyDeviceToHost));
   for (uint32_t i = 0; i < N; ++i)
@@ -645,6 +741,16 @@ int pg_set_field(pg_handle* h, int field, const double* in) {
     for (uint32_t c = 0; c < D; ++c) tmp[(size_t)i * S + c] = in[(size_t)i * D + c];
   CU(cudaMemcpy(dst, tmp.data(), tmp.size() * 8, cudaMemcpyHostToDevice));
   if (field == PG_FIELD_DISP) CU(cudaMemset(h->P.clamp_pending, 0, N));
+  if (h->precision == PG_MIXED && (field == PG_FIELD_DISP || field == PG_FIELD_ACC)) {
+    std::vector<float> tf;
+    if (field == PG_FIELD_DISP) {
+      pack_hl(in, N, D, nullptr, &tf);
+      CU(cudaMemcpy(h->P.disp_hl, tf.data(), tf.size() * 4, cudaMemcpyHostToDevice));
+    } else {
+      pack_f(in, N, D, &tf);
+      CU(cudaMemcpy(h->P.acc_f, tf.data(), tf.size() * 4, cudaMemcpyHostToDevice));
+    }
+  }
   return PG_OK;
 }
 

@@ -17,56 +17,11 @@
 
 #include <cmath>
 
+#include "pg_common.cuh"
 #include "pg_device.cuh"
 #include "pg_kernels.h"
 
 namespace pg {
-
-template <int D>
-struct Lay {
-  static constexpr int S = (D == 2) ? 2 : 4;   // doubles per node vector
-  static constexpr int SF = (D == 2) ? 2 : 4;  // floats per node vector (curf)
-};
-
-template <int D>
-__device__ __forceinline__ void ldv(const double* a, uint32_t i, double (&v)[D]) {
-  if constexpr (D == 2) {
-    double2 t = reinterpret_cast<const double2*>(a)[i];
-    v[0] = t.x;
-    v[1] = t.y;
-  } else {
-    const double2* p = reinterpret_cast<const double2*>(a + 4ull * i);
-    double2 t0 = p[0], t1 = p[1];
-    v[0] = t0.x;
-    v[1] = t0.y;
-    v[2] = t1.x;
-  }
-}
-template <int D>
-__device__ __forceinline__ void stv(double* a, uint32_t i, const double (&v)[D]) {
-  if constexpr (D == 2) {
-    reinterpret_cast<double2*>(a)[i] = make_double2(v[0], v[1]);
-  } else {
-    double2* p = reinterpret_cast<double2*>(a + 4ull * i);
-    p[0] = make_double2(v[0], v[1]);
-    p[1] = make_double2(v[2], 0.0);
-  }
-}
-template <int D>
-__device__ __forceinline__ void ldf(const float* a, uint32_t i, float (&v)[D]) {
-  if constexpr (D == 2) {
-    float2 t = reinterpret_cast<const float2*>(a)[i];
-    v[0] = t.x;
-    v[1] = t.y;
-  } else {
-    float4 t = reinterpret_cast<const float4*>(a)[i];
-    v[0] = t.x;
-    v[1] = t.y;
-    v[2] = t.z;
-  }
-}
-
-__device__ __forceinline__ void set_status(int32_t* st, int32_t code) { atomicCAS(st, 0, code); }
 
 // ---------------------------------------------------------------------------------------------
 // k_predict: disp += dt*vel + (dt*dt*0.5)*acc for movable grains; CurrPos = pos + disp.
@@ -164,174 +119,6 @@ __global__ void __launch_bounds__(256) k_predict(const Dev P) {
       atomicMax(&P.bbox[(size_t)g * 2 * D + D + c], kmax[c]);
     }
   }
-}
-
-// ---------------------------------------------------------------------------------------------
-// Exclusive scan of cell_count -> cell_start (reduce-then-scan, last block scans tile sums).
-// ---------------------------------------------------------------------------------------------
-constexpr int SCAN_THREADS = 1024;
-constexpr int SCAN_PER = 4;
-constexpr int SCAN_TILE = SCAN_THREADS * SCAN_PER;
-
-__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* warp_sums, uint32_t* total) {
-  const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  uint32_t x = v;
-  for (int off = 1; off < 32; off <<= 1) {
-    uint32_t y = __shfl_up_sync(0xffffffffu, x, off);
-    if (lane >= (uint32_t)off) x += y;
-  }
-  if (lane == 31) warp_sums[wid] = x;
-  __syncthreads();
-  if (wid == 0) {
-    uint32_t nw = blockDim.x >> 5;
-    uint32_t s = lane < nw ? warp_sums[lane] : 0;
-    for (int off = 1; off < 32; off <<= 1) {
-      uint32_t y = __shfl_up_sync(0xffffffffu, s, off);
-      if (lane >= (uint32_t)off) s += y;
-    }
-    if (lane < nw) warp_sums[lane] = s;
-  }
-  __syncthreads();
-  uint32_t base = wid ? warp_sums[wid - 1] : 0;
-  if (total) *total = warp_sums[(blockDim.x >> 5) - 1];
-  return base + x - v;
-}
-
-__global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(const Dev P) {
-  __shared__ uint32_t ws[32];
-  __shared__ bool last;
-  const uint32_t tile = blockIdx.x;
-  const uint32_t base = tile * SCAN_TILE + threadIdx.x * SCAN_PER;
-  uint32_t s = 0;
-  for (int k = 0; k < SCAN_PER; ++k) {
-    uint32_t i = base + k;
-    if (i < P.table_total) s += P.cell_count[i];
-  }
-  uint32_t tot;
-  block_excl_scan(s, ws, &tot);
-  if (threadIdx.x == 0) {
-    P.scan_tile_sum[tile] = tot;
-    __threadfence();
-    uint32_t ticket = atomicAdd(P.scan_done, 1u);
-    last = (ticket == gridDim.x - 1);
-  }
-  __syncthreads();
-  if (!last) return;
-  __threadfence();
-  // last block: exclusive scan of the tile sums in place
-  const uint32_t ntiles = gridDim.x;
-  uint32_t carry = 0;
-  for (uint32_t b0 = 0; b0 < ntiles; b0 += SCAN_THREADS) {
-    uint32_t i = b0 + threadIdx.x;
-    uint32_t v = i < ntiles ? ((volatile uint32_t*)P.scan_tile_sum)[i] : 0;
-    uint32_t t2;
-    uint32_t ex = block_excl_scan(v, ws, &t2);
-    __syncthreads();
-    if (i < ntiles) P.scan_tile_sum[i] = carry + ex;
-    carry += t2;
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) *P.scan_done = 0;
-}
-
-__global__ void __launch_bounds__(SCAN_THREADS) k_scan_final(const Dev P) {
-  __shared__ uint32_t ws[32];
-  const uint32_t tile = blockIdx.x;
-  const uint32_t base = tile * SCAN_TILE + threadIdx.x * SCAN_PER;
-  uint32_t v[SCAN_PER];
-  uint32_t s = 0;
-  for (int k = 0; k < SCAN_PER; ++k) {
-    uint32_t i = base + k;
-    v[k] = i < P.table_total ? P.cell_count[i] : 0;
-    s += v[k];
-  }
-  uint32_t ex = block_excl_scan(s, ws, nullptr) + P.scan_tile_sum[tile];
-  for (int k = 0; k < SCAN_PER; ++k) {
-    uint32_t i = base + k;
-    if (i < P.table_total) {
-      P.cell_start[i] = ex;
-      P.cell_count[i] = 0;  // ready for the next step's counting pass
-    }
-    ex += v[k];
-  }
-  if (tile == gridDim.x - 1 && threadIdx.x == blockDim.x - 1) P.cell_start[P.table_total] = P.N;
-}
-
-__global__ void __launch_bounds__(256) k_scatter(const Dev P) {
-  const uint32_t d = blockIdx.x * blockDim.x + threadIdx.x;
-  if (d < P.N) P.sorted[P.cell_start[P.cell_key[d]] + P.cell_rank[d]] = d;
-}
-
-// ---------------------------------------------------------------------------------------------
-// Torque centroid: mean_CurrPos (particle2.h:89-98) in the reference's serial order.
-// ---------------------------------------------------------------------------------------------
-template <int D>
-__global__ void k_torque_center(const Dev P) {
-  const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= P.G) return;
-  const GrainDev gr = P.grain[g];
-  double m[D];
-  for (int c = 0; c < D; ++c) m[c] = 0.0;
-  for (uint32_t i = gr.node_begin; i < gr.node_end; ++i) {
-    double cu[D];
-    ldv<D>(P.cur, i, cu);
-    for (int c = 0; c < D; ++c) m[c] = m[c] + cu[c];
-  }
-  double n = (double)(gr.node_end - gr.node_begin);
-  for (int c = 0; c < D; ++c) P.torque_c[(size_t)g * 3 + c] = m[c] / n;
-}
-
-// ---------------------------------------------------------------------------------------------
-// Fused force + integrate kernel (FP64 parity).
-// ---------------------------------------------------------------------------------------------
-template <int D>
-__device__ __forceinline__ void grain_box(const Dev& P, uint32_t g, double (&mn)[D], double (&mx)[D]) {
-  for (int c = 0; c < D; ++c) {
-    mn[c] = ordered_to_dbl(P.bbox[(size_t)g * 2 * D + c]);
-    mx[c] = ordered_to_dbl(P.bbox[(size_t)g * 2 * D + D + c]);
-  }
-}
-
-// intersects_box_fext (contact.h:984-1020), written per axis: (min_i - c <= max_j) && (max_i + c >= min_j)
-template <int D>
-__device__ __forceinline__ bool boxes_touch(const double (&mni)[D], const double (&mxi)[D],
-                                            const double (&mnj)[D], const double (&mxj)[D], double c) {
-  bool r = true;
-  for (int a = 0; a < D; ++a) r = r && ((mni[a] - c) <= mxj[a]) && ((mxi[a] + c) >= mnj[a]);
-  return r;
-}
-
-// within_interior_fext (contact.h:1066-1080) applied to get_minmax() and RectWall::lrtb()
-// arrays exactly as the reference indexes them (in 3D this reads the 6-entry arrays with the
-// 2D index pattern, as the reference does).
-template <int D>
-__device__ __forceinline__ bool within_interior(const double (&mn)[D], const double (&mx)[D],
-                                                const double* W, double c) {
-  double A[4];
-  if constexpr (D == 2) {
-    A[0] = mn[0]; A[1] = mx[0]; A[2] = mx[1]; A[3] = mn[1];
-  } else {
-    A[0] = mn[0]; A[1] = mn[1]; A[2] = mn[2]; A[3] = mx[0];
-  }
-  double AL = A[0] - c, AR = A[1] + c, AT = A[2] + c, AB = A[3] - c;
-  return (W[0] < AL) && (AR < W[1]) && (W[2] > AT) && (W[3] < AB);
-}
-
-template <int D>
-__device__ __forceinline__ void insert_cand(unsigned long long (&keys)[MAX_CAND], uint32_t (&idx)[MAX_CAND],
-                                            int& n, unsigned long long key, uint32_t q, const Dev& P) {
-  if (n >= (int)P.max_cand) {
-    set_status(P.status, PG_ECAPACITY);
-    return;
-  }
-  int k = n++;
-  while (k > 0 && keys[k - 1] > key) {
-    keys[k] = keys[k - 1];
-    idx[k] = idx[k - 1];
-    --k;
-  }
-  keys[k] = key;
-  idx[k] = q;
 }
 
 template <int D>
@@ -563,7 +350,8 @@ __global__ void __launch_bounds__(128) k_force(const Dev P) {
         rec.a_t1 = 0;
         rec.a_t2 = 0;
         rec.a_damp = 0;
-        rec.gid = d;
+        // replay key: the reference sums reactions grain by grain in its node-loop order
+        rec.gid = P.nl_bdry_only ? (gr.node_begin + P.bdry_rank[d]) : d;
         rec.side = (uint16_t)side;
         rec.has_fric = 0;
         rec.has_damp = 0;
@@ -692,119 +480,15 @@ __global__ void __launch_bounds__(128) k_force(const Dev P) {
 }
 
 // ---------------------------------------------------------------------------------------------
-// k_finalize: one block. Wall reactions in node order, pair log, wall move, step counter.
-// ---------------------------------------------------------------------------------------------
-template <int D>
-__global__ void __launch_bounds__(FINAL_THREADS) k_finalize(const Dev P) {
-  extern __shared__ unsigned long long skey[];
-  constexpr int NS = 2 * D;
-  const uint32_t tid = threadIdx.x;
-  const uint32_t t = *P.step;
-  const uint32_t R = *P.wrec_count;
-  const uint32_t nrx = P.I * NS * D;
-  for (uint32_t i = tid; i < nrx; i += blockDim.x) P.reaction[i] = 0.0;
-  if (R > 0) {
-    if (R > (uint32_t)WREC_SMEM_CAP || R > P.wrec_cap) {
-      if (tid == 0) set_status(P.status, PG_ECAPACITY);
-    } else {
-      uint32_t n2 = 32;
-      while (n2 < R) n2 <<= 1;
-      for (uint32_t i = tid; i < n2; i += blockDim.x) {
-        if (i < R) {
-          const WallRec& r = P.wrec[i];
-          skey[i] = ((unsigned long long)r.gid << 32) | ((unsigned long long)r.side << 28) | i;
-        } else {
-          skey[i] = ~0ull;
-        }
-      }
-      __syncthreads();
-      for (uint32_t k = 2; k <= n2; k <<= 1) {
-        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
-          for (uint32_t i = tid; i < n2; i += blockDim.x) {
-            uint32_t l = i ^ j;
-            if (l > i) {
-              unsigned long long a = skey[i], b = skey[l];
-              bool up = ((i & k) == 0);
-              if ((a > b) == up) {
-                skey[i] = b;
-                skey[l] = a;
-              }
-            }
-          }
-          __syncthreads();
-        }
-      }
-      for (uint32_t p = tid; p < P.I * NS; p += blockDim.x) {
-        const uint32_t inst = p / NS, side = p % NS;
-        const unsigned long long lo_key = (unsigned long long)P.inst[inst].node_begin << 32;
-        const unsigned long long hi_key = (unsigned long long)P.inst[inst].node_end << 32;
-        uint32_t lo = 0, hi = R;
-        while (lo < hi) {
-          uint32_t mid = (lo + hi) >> 1;
-          if (skey[mid] < lo_key) lo = mid + 1; else hi = mid;
-        }
-        double r[3] = {0.0, 0.0, 0.0};
-        bool any = false;
-        for (uint32_t k = lo; k < R && skey[k] < hi_key; ++k) {
-          if (((skey[k] >> 28) & 0xfu) != side) continue;
-          const WallRec& w = P.wrec[skey[k] & 0x0fffffffu];
-          const int dir = (D == 2) ? ((side == 0 || side == 1) ? 0 : 1) : (int)(side % 3);
-          r[dir] = r[dir] - w.a_normal;
-          if (w.has_fric) {
-            if constexpr (D == 2) {
-              const int tg = (dir + 1) % 2;
-              r[tg] = r[tg] - w.a_t1;
-            } else {
-              r[(dir + 1) % 3] = r[(dir + 1) % 3] - w.a_t1;
-              r[(dir + 2) % 3] = r[(dir + 2) % 3] - w.a_t2;
-            }
-          }
-          if (w.has_damp) r[dir] = r[dir] - w.a_damp;
-          any = true;
-        }
-        if (any) {
-          for (int c = 0; c < D; ++c) P.reaction[((size_t)inst * NS + side) * D + c] = r[c];
-        }
-      }
-    }
-  }
-  __syncthreads();
-  if (tid == 0) {
-    if (P.record_pairs) {
-      const uint32_t slot = (t - 1) % P.log_cap;
-      P.log_count[slot] = P.pair_acc[0];
-      P.log_hash[slot] = P.pair_acc[1];
-      P.pair_acc[0] = 0;
-      P.pair_acc[1] = 0;
-    }
-    *P.wrec_count = 0;
-    *P.step = t + 1;
-  }
-  for (uint32_t p = tid; p < P.I * NS; p += blockDim.x) {
-    InstDev* in = &P.inst[p / NS];
-    const int s = p % NS;
-    in->wall[s] = in->wall[s] + in->wall_speed[s] * P.dt;
-  }
-  for (uint32_t i = tid; i < P.G * NS; i += blockDim.x) {
-    P.bbox[i] = ((i % NS) < (uint32_t)D) ? ~0ull : 0ull;
-  }
-}
-
-// ---------------------------------------------------------------------------------------------
 // host-side launchers
 // ---------------------------------------------------------------------------------------------
-static inline uint32_t cdiv(uint32_t a, uint32_t b) { return (a + b - 1) / b; }
-
 template <int D>
 static void launch_step_t(const Dev& P, const LaunchCfg& L, cudaStream_t s, uint64_t* launches,
                           cudaEvent_t e0 = nullptr, cudaEvent_t e1 = nullptr) {
   const uint32_t nthr_nodes = P.n_chunks * 32;
   k_predict<D><<<cdiv(P.N, 256), 256, 0, s>>>(P);
-  const uint32_t ntiles = cdiv(P.table_total, SCAN_TILE);
-  k_scan_reduce<<<ntiles, SCAN_THREADS, 0, s>>>(P);
-  k_scan_final<<<ntiles, SCAN_THREADS, 0, s>>>(P);
-  k_scatter<<<cdiv(P.N, 256), 256, 0, s>>>(P);
-  *launches += 4;
+  *launches += 1;
+  launch_grid_build(P, s, launches);
   if (P.enable_torque) {
     k_torque_center<D><<<cdiv(P.G, 128), 128, 0, s>>>(P);
     *launches += 1;

@@ -1,0 +1,17 @@
+// Host-side entry points of the mixed-precision kernels (pg_kernels_mixed.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "pg_device.cuh"
+#include "pg_kernels.h"
+
+namespace pg {
+
+cudaError_t kernels_mixed_init();
+// Enqueue one mixed-precision time step; e0/e1 (may be null) bracket the force kernel.
+void launch_step_mixed(const Dev& P, const LaunchCfg& L, cudaStream_t s, uint64_t* launches,
+                       cudaEvent_t e0 = nullptr, cudaEvent_t e1 = nullptr);
+
+}  // namespace pg

@@ -64,6 +64,12 @@ class Simulation:
     def step(self, n=1):
         N.check(N.lib().pg_step(self.h, int(n)))
 
+    def step_timed(self, n):
+        """Advance n steps; returns the device time in ms (CUDA events on the engine's stream)."""
+        ms = C.c_double()
+        N.check(N.lib().pg_step_timed(self.h, int(n), C.byref(ms)))
+        return ms.value
+
     def synchronize(self):
         N.check(N.lib().pg_synchronize(self.h))
 
@@ -140,6 +146,10 @@ def run_simulation(root=".", dim=2, precision="fp64"):
     writes <root>/output/hdf5/."""
     p = N.PG_MIXED if precision == "mixed" else N.PG_FP64
     N.check(N.lib().pg_run_simulation(str(root).encode(), int(dim), p))
+
+
+def select_device(device):
+    N.check(N.lib().pg_select_device(int(device)))
 
 
 def device_count():

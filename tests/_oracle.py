@@ -42,6 +42,7 @@ def oracle_lib():
         L.orc_get_pair_log.argtypes = [C.c_void_p, N.u64p, N.u64p]
         L.orc_too_close.argtypes = [C.c_void_p]
         L.orc_too_close.restype = C.c_uint64
+        L.orc_set_mode.argtypes = [C.c_void_p, C.c_int, C.c_int]
         _lib = L
     return _lib
 
@@ -74,6 +75,9 @@ class OracleSim:
         if getattr(self, "h", None):
             oracle_lib().orc_destroy(self.h)
             self.h = None
+
+    def set_mode(self, reference_structured=0, threads=1):
+        oracle_lib().orc_set_mode(self.h, int(reference_structured), int(threads))
 
     def step(self, n=1):
         oracle_lib().orc_step(self.h, int(n))
@@ -160,7 +164,7 @@ def run_reference(case_dir, dim, timeout=600):
     if not os.path.exists(exe):
         raise FileNotFoundError("reference build unavailable: %s" % exe)
     r = subprocess.run([exe], cwd=case_dir, capture_output=True, text=True, timeout=timeout,
-                       env=dict(os.environ, OMP_NUM_THREADS="1"))
+                       env=dict(os.environ, OMP_NUM_THREADS=os.environ.get("PERIGRAIN_REF_THREADS", "2")))
     if r.returncode != 0:
         raise RuntimeError("reference run failed (%d):\n%s\n%s" % (r.returncode, r.stdout[-3000:], r.stderr[-3000:]))
     return r.stdout
@@ -198,3 +202,73 @@ def conn_from_alive(setup, alive):
         noff[1:] = np.cumsum(keep_counts)
         res.append(rows_to_conn(noff, loc[a]).astype(np.uint32))
     return res
+
+
+def drive(sim, conf, n_grains, on_snapshot):
+    """The run_timeloop step loop (timeloop.h:608-1006) around any engine with the Simulation
+    interface: hooks at the start of step t, on_snapshot(counter) every `modulo` steps."""
+    T, mod = int(conf["timesteps"]), int(conf["modulo"])
+    hooks = {}
+    if conf.get("set_movable_index", -1) != -1:
+        hooks.setdefault(int(conf["set_movable_timestep"]), []).append(("movable", int(conf["set_movable_index"])))
+    if conf.get("set_stoppable_index", -1) != -1:
+        hooks.setdefault(int(conf["set_stoppable_timestep"]), []).append(("stoppable", int(conf["set_stoppable_index"])))
+    counter = 1
+    t = 1
+    while t <= T:
+        for kind, g in hooks.get(t, []):
+            if kind == "movable":
+                sim.set_grain_flags(g, movable=1)
+            else:
+                sim.set_grain_flags(g, stoppable=1)
+        e = min(T, ((t + mod - 1) // mod) * mod)
+        for ht in hooks:
+            if t < ht <= e:
+                e = ht - 1
+        sim.step(e - t + 1)
+        t = e + 1
+        if conf.get("save_file", 1) and e % mod == 0:
+            on_snapshot(counter)
+            counter += 1
+
+
+def engine_kwargs(conf):
+    return dict(dt=float(conf["dt"]), enable_fracture=int(conf.get("enable_fracture", 0)),
+                nl_bdry_only=int(conf.get("nl_bdry_only", 0)), allow_damping=int(conf.get("allow_damping", 1)),
+                allow_friction=int(conf.get("allow_friction", 1)), self_contact=int(conf.get("self_contact", 1)),
+                enable_torque=int(conf.get("enable_torque", 0)),
+                gradient_extforce=int(conf.get("gradient_extforce", 0)),
+                extforce_maxstep=int(conf.get("extforce_maxstep", 0)))
+
+
+def load_golden(name):
+    import json
+
+    z = np.load(os.path.join(ROOT, "tests", "golden", name + ".npz"))
+    meta = json.loads(bytes(z["meta"]).decode())
+    return z, meta
+
+
+def resumed_setup(s, tc, wall_info=None, reload_connectivity=True):
+    """The state run_timeloop rebuilds on resume (timeloop.h:508-550): disp = CurrPos - pos, vel
+    and acc from tc_%05u.h5, neighbour rows from its Connectivity (conn2NArr), wall from wall_."""
+    from perigrain_gb300.setups import conn_to_rows
+
+    r = s.copy()
+    D = s.dim
+    r.disp = (tc["CurrPos"] - s.pos.reshape(-1, D)).reshape(-1)
+    r.vel = tc["vel"].reshape(-1).copy()
+    r.acc = tc["acc"].reshape(-1).copy()
+    if reload_connectivity:
+        offs, locs, base = [np.zeros(1, np.uint64)], [], 0
+        for g in range(s.n_grains):
+            n = int(s.grain_node_offset[g + 1] - s.grain_node_offset[g])
+            off, loc = conn_to_rows(tc["Connectivity"][g], n)
+            offs.append(off[1:] + np.uint64(base))
+            locs.append(loc)
+            base += int(off[-1])
+        r.bond_offset = np.concatenate(offs).astype(np.uint64)
+        r.bond_local = np.concatenate(locs).astype(np.uint32)
+    if wall_info is not None:
+        r.wall_geom = np.asarray(wall_info, np.float64).ravel().copy()
+    return r

@@ -1,0 +1,43 @@
+"""The oracle (C++ restatement) reproduces the reference's own outputs bit for bit.
+
+Golden fixtures: tests/golden/*.npz, written by tests/golden/make_golden.py from runs of the
+reference simulator (its src/ headers and run/ drivers compiled unmodified against API shims).
+They hold CurrPos, vel, acc, force, Connectivity, wall_info and wall reaction of every snapshot.
+"""
+import platform
+
+import numpy as np
+import pytest
+
+import _oracle as O
+from golden.make_golden import CASES, case_setup, setup_digest
+
+# pow/asin in the wall force come from the host libm; the fixtures were written on x86-64
+WALL_CASES = {"wall2d_full", "wall3d"}
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_oracle_matches_reference_outputs(name):
+    z, meta = O.load_golden(name)
+    s = case_setup(CASES[name])
+    assert setup_digest(s) == meta["digest"], "setup generator drifted from the fixture"
+    conf = meta["conf"]
+    sim = O.OracleSim(s, **O.engine_kwargs(conf))
+    exact = name not in WALL_CASES or platform.machine() == "x86_64"
+
+    def check(k):
+        for f in ("CurrPos", "vel", "acc", "force"):
+            a, b = sim.field(f), z["%d/%s" % (k, f)]
+            if exact:
+                assert np.array_equal(a, b), (name, k, f, np.abs(a - b).max())
+            else:
+                assert np.abs(a - b).max() <= 1e-9 * np.abs(b).max(), (name, k, f)
+        assert np.array_equal(sim.wall()[0], z["%d/wall_info" % k])
+        r = sim.reaction()[0]
+        if exact:
+            assert np.array_equal(r, z["%d/reaction" % k])
+        conn = O.conn_from_alive(s, sim.bond_alive())
+        for g in range(s.n_grains):
+            assert np.array_equal(conn[g], z["%d/conn%d" % (k, g)]), (name, k, g)
+
+    O.drive(sim, conf, s.n_grains, check)
