@@ -7,9 +7,14 @@ all advanced together in one handle. A "step" is one time step of every instance
     python bench.py [--gpus N] [--steps K] [--warmup W] [--workload 0..4] [--precision fp64|mixed]
     python bench.py --impl reference ...   # the reference's CPU algorithm on the host cores
 
-Prints one JSON line (rank 0). `value` is device-timed (CUDA events on the engine's stream, state
-resident in HBM, inputs larger than L2); `e2e` goes through the C ABI from host buffers: setup
-upload + the timed steps + a tc_-snapshot download (CurrPos, vel, acc, force) every 100 steps.
+Prints one JSON line (rank 0). `value` is the mixed-precision batched path (FP32 forces, FP64
+state), device-timed (CUDA events on the engine's stream, state resident in HBM, inputs larger
+than L2), with block size and grid density picked by the project autotuner. Beside it: the plain
+FP64 path on the same batch (`plain_fp64`), 256 sequential single-instance FP64 runs
+(`sequential_fp64`, timed on a sample of instances), the mixed-vs-FP64 position error after the
+same steps and the FP64 perturbation floor of these chaotic dynamics (`accuracy`). `e2e` goes
+through the C ABI from host buffers: setup upload + the timed steps + a tc_-snapshot download
+(CurrPos, vel, acc, force) every 100 steps.
 """
 import argparse
 import json
@@ -25,14 +30,23 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "node-steps/s"
-# dominant kernel: fused bond + contact + wall + integrate (k_force); per node it reads disp, xpos,
-# cur, vel, acc, extforce (dim doubles each), vol, grain id, degree, and writes acc, vel, force;
-# per directed bond it reads the neighbour id (4 B), xi_norm (8 B) and one alive bit.
-BOND_BYTES = 12.125
+# Algorithmic bytes of the dominant kernel (the fused bond + contact + wall + integrate kernel),
+# counting each array once per launch and treating neighbour gathers as cache-served:
+#   FP64:  per node  reads disp, xpos, cur, vel, acc, extforce (8*dim B each), vol (8), grain id
+#          and degree (4 + 4); writes acc, vel, force (8*dim each) -> 72*dim + 16 B
+#          per bond  neighbour id (4 B) + xi_norm (8 B) + one alive bit          -> 12.125 B
+#   mixed: per node  reads FP32 hi/lo disp, xpos, cur (8*dim each), FP64 vel (8*dim), FP32 acc and
+#          extforce (4*dim each), grain id (4); writes FP32 acc (4*dim), FP64 vel (8*dim),
+#          FP32 force (4*dim)                                                    -> 56*dim + 4 B
+#          per bond  neighbour id (4 B) + one alive bit                          -> 4.125 B
 
 
-def node_bytes(dim):
-    return 9 * 8 * dim + 8 + 8
+def node_bytes(dim, precision="fp64"):
+    return 72 * dim + 16 if precision == "fp64" else 56 * dim + 4
+
+
+def bond_bytes(precision="fp64"):
+    return 12.125 if precision == "fp64" else 4.125
 
 
 def fp64_flops_per_bond(dim):
@@ -126,38 +140,47 @@ def engine_kwargs(spec, precision):
     return dict(dt=spec["dt"], enable_fracture=1, precision=precision)
 
 
-def cpu_reference(setup, spec, steps, threads, budget_s=20.0):
-    """The reference's CPU algorithm, timed on a bounded sample of the workload: the oracle port
-    in reference-structured mode (the reference's node-pair loops, bit-identical arithmetic),
-    independent instances run concurrently on `threads` host threads."""
-    sys.path.insert(0, os.path.join(ROOT, "tests"))
-    import _oracle as O
-    from perigrain_gb300 import setups
-
-    take = min(setup.n_instances, max(1, threads))
-    # sub-setup made of the first `take` instances
-    g_end = int(np.searchsorted(setup.grain_instance, take))
-    n_end = int(setup.grain_node_offset[g_end])
-    sub = setup.copy()
-    sub.grain_instance = setup.grain_instance[:g_end]
-    sub.grain_node_offset = setup.grain_node_offset[: g_end + 1]
+def instance_subset(setup, first, count):
+    """Single setup made of instances [first, first + count) of a batched setup."""
     D = setup.dim
+    g0 = int(np.searchsorted(setup.grain_instance, first))
+    g1 = int(np.searchsorted(setup.grain_instance, first + count))
+    n0, n1 = int(setup.grain_node_offset[g0]), int(setup.grain_node_offset[g1])
+    b0, b1 = int(setup.bond_offset[n0]), int(setup.bond_offset[n1])
+    sub = setup.copy()
+    sub.grain_instance = setup.grain_instance[g0:g1] - np.uint32(first)
+    sub.grain_node_offset = setup.grain_node_offset[g0:g1 + 1] - np.uint32(n0)
     for f in ("pos", "disp", "vel", "acc", "extforce"):
-        setattr(sub, f, getattr(setup, f)[: n_end * D])
-    sub.vol = setup.vol[:n_end]
-    sub.bond_offset = setup.bond_offset[: n_end + 1]
-    sub.bond_local = setup.bond_local[: int(setup.bond_offset[n_end])]
-    sub.bdry_offset = setup.bdry_offset[: g_end + 1]
-    sub.bdry_nodes = setup.bdry_nodes[: int(setup.bdry_offset[g_end])]
-    sub.clamped_offset = setup.clamped_offset[: g_end + 1]
-    sub.clamped_nodes = setup.clamped_nodes[: int(setup.clamped_offset[g_end])]
+        setattr(sub, f, getattr(setup, f)[n0 * D:n1 * D].copy())
+    sub.vol = setup.vol[n0:n1].copy()
+    sub.bond_offset = setup.bond_offset[n0:n1 + 1] - np.uint64(b0)
+    sub.bond_local = setup.bond_local[b0:b1].copy()
+    d0, d1 = int(setup.bdry_offset[g0]), int(setup.bdry_offset[g1])
+    sub.bdry_offset = setup.bdry_offset[g0:g1 + 1] - np.uint32(d0)
+    sub.bdry_nodes = setup.bdry_nodes[d0:d1].copy()
+    c0, c1 = int(setup.clamped_offset[g0]), int(setup.clamped_offset[g1])
+    sub.clamped_offset = setup.clamped_offset[g0:g1 + 1] - np.uint32(c0)
+    sub.clamped_nodes = setup.clamped_nodes[c0:c1].copy()
     for f in ("delta", "rho", "cnot", "snot", "movable", "breakable", "stoppable", "break_bonds", "torque_axis",
               "torque_val"):
-        setattr(sub, f, getattr(setup, f)[:g_end])
+        setattr(sub, f, getattr(setup, f)[g0:g1].copy())
     for f in ("contact_radius", "normal_stiffness", "friction_coefficient", "damping_ratio", "allow_wall"):
-        setattr(sub, f, getattr(setup, f)[:take])
-    sub.wall_geom = setup.wall_geom[: take * 2 * D]
-    sub.wall_speed = setup.wall_speed[: take * 2 * D]
+        setattr(sub, f, getattr(setup, f)[first:first + count].copy())
+    sub.wall_geom = setup.wall_geom[first * 2 * D:(first + count) * 2 * D].copy()
+    sub.wall_speed = setup.wall_speed[first * 2 * D:(first + count) * 2 * D].copy()
+    return sub
+
+
+def cpu_reference(setup, spec, steps, threads, budget_s=12.0):
+    """The reference's CPU algorithm, timed on a bounded sample of the workload: the oracle port
+    in reference-structured mode (the reference's node-pair loops, bit-identical arithmetic),
+    independent instances run concurrently on `threads` host threads, for up to `steps` steps or
+    until `budget_s` seconds of work have been done."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import _oracle as O
+
+    take = min(setup.n_instances, max(1, threads))
+    sub = instance_subset(setup, 0, take)
     sim = O.OracleSim(sub, dt=spec["dt"], enable_fracture=1)
     sim.set_mode(1, threads)
     t0 = time.perf_counter()
@@ -178,9 +201,9 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--workload", type=int, default=3)
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--cpu-steps", type=int, default=5)
+    ap.add_argument("--cpu-steps", type=int, default=400)
     ap.add_argument("--profile-run", action="store_true",
                     help="only warmup + steps of the engine (the command profiled under ncu)")
     a = ap.parse_args()
@@ -220,7 +243,8 @@ def main():
 
     setup, spec = build_workload(a.workload, rank)
     kw = engine_kwargs(spec, a.precision)
-    sim = Simulation(setup, **kw)
+    sim = Simulation(setup, autotune=not a.profile_run, **kw)
+    tuned = sim.launch_config()
     sim.step(a.warmup)
     sim.synchronize()
     if a.profile_run:
@@ -259,7 +283,51 @@ def main():
     st, _ = sim.device_status()
     if st:
         raise RuntimeError("device status %d after the timed region" % st)
+    total_steps = a.warmup + 2 * a.steps
+    x_main = sim.field("CurrPos")
     sim.close()
+
+    plain = seq = accuracy = None
+    if a.precision == "mixed" and rank == 0:
+        # the plain FP64 path on the same batch, same steps (FP64 = the reference's arithmetic)
+        s64 = Simulation(setup, **engine_kwargs(spec, "fp64"))
+        s64.step(a.warmup)
+        ms64 = s64.step_timed(a.steps)
+        s64.set_timing(True)
+        s64.step(a.steps)
+        f64_ms, t64_ms, n64 = s64.kernel_times()
+        x64 = s64.field("CurrPos")
+        s64.close()
+        plain = {"value": setup.n_nodes * a.steps / (ms64 / 1e3), "unit": METRIC, "ms_per_step": ms64 / a.steps,
+                 "k_force_ms": f64_ms / max(1, n64),
+                 "fp64_tflops": setup.n_bonds * fp64_flops_per_bond(setup.dim) / (f64_ms / max(1, n64) / 1e3) / 1e12}
+        # chaos floor: FP64 again with one velocity component changed by one ulp
+        sp = setup.copy()
+        k = int(setup.grain_node_offset[1]) * setup.dim
+        sp.vel[k] = np.nextafter(sp.vel[k], np.inf)
+        sf = Simulation(sp, **engine_kwargs(spec, "fp64"))
+        sf.step(total_steps)
+        xf = sf.field("CurrPos")
+        sf.close()
+        scale = np.abs(x64).max()
+        accuracy = {"steps": total_steps, "pos_rel_err_mixed_vs_fp64": float(np.abs(x_main - x64).max() / scale),
+                    "fp64_one_ulp_perturbation_floor": float(np.abs(xf - x64).max() / scale),
+                    "note": "max|dx| / max|x| over all nodes; the FP64 engine is bit-identical to the "
+                            "reference's arithmetic (tests), the floor is FP64 vs FP64 with one velocity "
+                            "component moved by one ulp"}
+        # 256 sequential single-instance FP64 runs, timed on a sample of instances
+        ns = min(8, setup.n_instances)
+        t_seq, nodes_seq = 0.0, 0
+        for i in range(ns):
+            one = instance_subset(setup, i, 1)
+            si = Simulation(one, **engine_kwargs(spec, "fp64"))
+            si.step(a.warmup)
+            t_seq += si.step_timed(a.steps)
+            nodes_seq += one.n_nodes
+            si.close()
+        seq = {"value": nodes_seq * a.steps / (t_seq / 1e3), "unit": METRIC,
+               "sample": "%d instances run one after another, %d steps each" % (ns, a.steps),
+               "est_ms_for_all_instances_per_step": t_seq / a.steps * setup.n_instances / ns}
 
     # end to end through the C ABI from host buffers
     t0 = time.perf_counter()
@@ -284,7 +352,7 @@ def main():
     D = setup.dim
     peak, peak_kind = load_peaks()
     force_launch_ms = force_ms / max(1, nforce)
-    alg_bytes = setup.n_nodes * node_bytes(D) + setup.n_bonds * BOND_BYTES
+    alg_bytes = setup.n_nodes * node_bytes(D, a.precision) + setup.n_bonds * bond_bytes(a.precision)
     achieved = alg_bytes / (force_launch_ms / 1e3) / 1e9
     fp64_tflops = setup.n_bonds * fp64_flops_per_bond(D) / (force_launch_ms / 1e3) / 1e12
     traffic = profiled_traffic("%s/%s" % (spec["name"], a.precision))
@@ -292,17 +360,18 @@ def main():
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": ms_max / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if a.precision == "fp64" else "f32-forces/f64-state", "data": "synthetic",
+        "dtype": "f64" if a.precision == "fp64" else "f32-forces/f64-state", "data": "synthetic (seeded generator)",
         "config": {"workload": spec["name"], "precision": a.precision, "instances": setup.n_instances,
                    "nodes": setup.n_nodes, "bonds": setup.n_bonds, "dim": D, "dt": spec["dt"],
                    "parallelism": "instances per GPU" if world == 1 else "dp%d (independent ensembles)" % world,
                    "l2": "inputs larger than L2 (%.0f MB of node and bond arrays resident)"
                          % ((alg_bytes + setup.n_bonds * 4) / 1e6)},
-        "roofline": {"bound": "hbm", "kernel": "k_force", "achieved": achieved, "peak": peak, "unit": "GB/s",
+        "roofline": {"bound": "hbm", "kernel": "k_force" if a.precision == "fp64" else "k_force_mx",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
                      "algorithmic_bytes_per_launch": alg_bytes, "launch_ms": force_launch_ms,
                      "share_of_step": force_ms / total_ms if total_ms else None,
-                     "fp64_tflops": fp64_tflops, "fp64_nominal_tflops": 1.25},
+                     **({"fp64_tflops": fp64_tflops, "fp64_nominal_tflops": 1.25} if a.precision == "fp64" else {})},
         "cpu_baseline": {"value": cpu_v, "unit": METRIC, "cores": cpu_info["cores"], "kind": cpu_info["kind"],
                          "sample": "%d instances x %d steps of %s (%d nodes), reference-structured oracle port, "
                                    "%.1f s" % (cpu_info["instances"], cpu_info["steps"], spec["name"],
@@ -312,6 +381,10 @@ def main():
                 "note": "pg_create from host arrays + %d steps + %d tc_ snapshot downloads" % (a.steps, snaps)},
         "gpu_launches": launches,
         "clocks": clk.summary(),
+        "autotuned": tuned,
+        "plain_fp64": plain,
+        "sequential_fp64": seq,
+        "accuracy": accuracy,
     }
     print(json.dumps(line), flush=True)
     if dist:

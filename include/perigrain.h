@@ -115,7 +115,9 @@ typedef struct pg_config {
   uint32_t pair_log_capacity; /* steps kept in the pair log ring (default 1024 when 0) */
   uint32_t first_step;     /* t of the first step taken (1, or resume_ind*modulo + 1) */
   uint32_t max_contacts;   /* per-node contact candidate capacity (default 48 when 0) */
-  uint32_t block_size;     /* threads per block for node kernels (0: autotuned default) */
+  uint32_t block_size;     /* threads per block of the fused force kernel (0: default 128) */
+  int32_t autotune;        /* 1: pick block_size and cells_per_node by timing trial runs */
+  uint32_t cells_per_node; /* contact-grid capacity per node (0: 4 in 2D, 8 in 3D) */
 } pg_config;
 
 /* ---- lifecycle ---------------------------------------------------------------------------- */
@@ -178,6 +180,8 @@ int pg_get_pair_log(pg_handle* h, uint32_t n, uint64_t* count, uint64_t* hash);
 /* Sticky device error word (PG_ECAPACITY/PG_ERANGE/...), 0 if none; also "nodes too close"
  * events (dir_norm == 0 in contact.h:737) counted since creation. */
 int pg_get_device_status(pg_handle* h, int32_t* status, uint64_t* too_close_events);
+/* Launch configuration in use (after autotuning): force-kernel block size, grid cells per node. */
+int pg_get_launch_config(pg_handle* h, uint32_t* block_size, uint32_t* cells_per_node);
 /* Number of kernel launches issued by the last pg_step call. */
 int pg_get_launch_count(pg_handle* h, uint64_t* launches);
 /* Per-kernel device time of the last pg_step call (CUDA events; needs timing enabled). */

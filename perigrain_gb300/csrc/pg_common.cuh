@@ -94,9 +94,14 @@ static __global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(const Dev P
   const uint32_t tile = blockIdx.x;
   const uint32_t base = tile * SCAN_TILE + threadIdx.x * SCAN_PER;
   uint32_t s = 0;
-  for (int k = 0; k < SCAN_PER; ++k) {
-    uint32_t i = base + k;
-    if (i < P.table_total) s += P.cell_count[i];
+  if (base + SCAN_PER <= P.table_total) {
+    const uint4 v = *reinterpret_cast<const uint4*>(P.cell_count + base);
+    s = v.x + v.y + v.z + v.w;
+  } else {
+    for (int k = 0; k < SCAN_PER; ++k) {
+      uint32_t i = base + k;
+      if (i < P.table_total) s += P.cell_count[i];
+    }
   }
   uint32_t tot;
   block_excl_scan(s, ws, &tot);
@@ -131,19 +136,38 @@ static __global__ void __launch_bounds__(SCAN_THREADS) k_scan_final(const Dev P)
   const uint32_t base = tile * SCAN_TILE + threadIdx.x * SCAN_PER;
   uint32_t v[SCAN_PER];
   uint32_t s = 0;
-  for (int k = 0; k < SCAN_PER; ++k) {
-    uint32_t i = base + k;
-    v[k] = i < P.table_total ? P.cell_count[i] : 0;
-    s += v[k];
-  }
-  uint32_t ex = block_excl_scan(s, ws, nullptr) + P.scan_tile_sum[tile];
-  for (int k = 0; k < SCAN_PER; ++k) {
-    uint32_t i = base + k;
-    if (i < P.table_total) {
-      P.cell_start[i] = ex;
-      P.cell_count[i] = 0;  // ready for the next step's counting pass
+  const bool full = base + SCAN_PER <= P.table_total;
+  if (full) {
+    const uint4 q = *reinterpret_cast<const uint4*>(P.cell_count + base);
+    v[0] = q.x;
+    v[1] = q.y;
+    v[2] = q.z;
+    v[3] = q.w;
+  } else {
+    for (int k = 0; k < SCAN_PER; ++k) {
+      uint32_t i = base + k;
+      v[k] = i < P.table_total ? P.cell_count[i] : 0;
     }
+  }
+  for (int k = 0; k < SCAN_PER; ++k) s += v[k];
+  uint32_t ex = block_excl_scan(s, ws, nullptr) + P.scan_tile_sum[tile];
+  uint32_t st[SCAN_PER];
+  for (int k = 0; k < SCAN_PER; ++k) {
+    st[k] = ex;
     ex += v[k];
+  }
+  if (full) {
+    // cell_start has table_total + 1 entries, so base need not be 16-byte aligned: plain stores
+    for (int k = 0; k < SCAN_PER; ++k) P.cell_start[base + k] = st[k];
+    *reinterpret_cast<uint4*>(P.cell_count + base) = make_uint4(0, 0, 0, 0);  // next step's counts
+  } else {
+    for (int k = 0; k < SCAN_PER; ++k) {
+      uint32_t i = base + k;
+      if (i < P.table_total) {
+        P.cell_start[i] = st[k];
+        P.cell_count[i] = 0;
+      }
+    }
   }
   if (tile == gridDim.x - 1 && threadIdx.x == blockDim.x - 1) P.cell_start[P.table_total] = P.N;
 }
@@ -316,6 +340,22 @@ static __global__ void __launch_bounds__(FINAL_THREADS) k_finalize(const Dev P) 
     const int s = p % NS;
     in->wall[s] = in->wall[s] + in->wall_speed[s] * P.dt;
   }
+  // refit every instance's grid to this step's bounding box for the next step
+  for (uint32_t k = tid; k < P.I; k += blockDim.x) {
+    InstDev* in = &P.inst[k];
+    if (in->grain_end <= in->grain_begin) continue;
+    double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+    bool ok = true;
+    for (int c = 0; c < D; ++c) {
+      lo[c] = ordered_to_dbl(P.ibox[(size_t)k * NS + c]);
+      hi[c] = ordered_to_dbl(P.ibox[(size_t)k * NS + D + c]);
+      ok = ok && isfinite(lo[c]) && isfinite(hi[c]);
+      P.ibox[(size_t)k * NS + c] = ~0ull;
+      P.ibox[(size_t)k * NS + D + c] = 0ull;
+    }
+    if (ok) fit_grid(*in, D, lo, hi);
+  }
+  __syncthreads();
   for (uint32_t i = tid; i < P.G * NS; i += blockDim.x) {
     P.bbox[i] = ((i % NS) < (uint32_t)D) ? ~0ull : 0ull;
   }

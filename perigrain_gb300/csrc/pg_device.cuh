@@ -10,9 +10,11 @@
 //     NbdArr order; padding slots are never alive;
 //   * the alive set is one 32-bit word per (chunk, k): bit `lane` is bond k of that lane, so a
 //     warp reads its alive bits with one broadcast load and writes them back with one ballot;
-//   * the contact grid is a per-instance hashed uniform grid (cell >= R_c) rebuilt every step by
-//     a counting sort of the nodes by bucket (one radix digit that spans the whole bucket range),
-//     whose exclusive scan doubles as the cell-start table.
+//   * the contact grid is a dense row-major uniform grid per instance (cell >= 1.0625 R_c), refitted
+//     on the device every step to the instance's bounding box (plus two cells) and rebuilt by a
+//     counting sort of the nodes by cell (one radix digit spanning all cells), whose exclusive scan
+//     doubles as the cell-start table. Cell coordinates are clamped to the grid, so a node that
+//     moves outside the box still lands in an edge cell and every pair within R_c is still found.
 #pragma once
 #include <cstdint>
 
@@ -44,17 +46,56 @@ struct GrainDev {
 
 struct InstDev {
   double contact_rad, normal_stiffness, friction_coefficient, damping_ratio;
-  double origin[3];
-  double cell;          // grid cell edge (>= contact_rad)
+  double origin[3];     // lower corner of this step's grid
+  double xorigin[3];    // fixed origin of the FP32 hi/lo bond reference positions (mixed path)
+  double cell;          // grid cell edge (>= 1.0625 contact_rad)
+  double cell_min;      // smallest admissible cell edge
   float inv_cell_f;     // 1/cell in float (cell coordinates are computed in FP32)
   float cell_f;
-  float range_f;        // |x - origin| beyond this cannot be resolved in FP32 -> PG_ERANGE
-  uint32_t table_off, table_mask;
-  uint32_t node_begin, node_end;
+  float pre_f;          // FP32 prefilter radius of contact candidates (1.0625 contact_rad)
+  uint32_t dims[3];     // cells per axis (dims[2] = 1 in 2D)
+  uint32_t table_off, table_cap;
+  uint32_t node_begin, node_end, grain_begin, grain_end;
   int32_t allow_wall;
   double wall[6];
   double wall_speed[6];
 };
+
+// Fit the grid of one instance to the node bounding box [lo, hi] plus two cells on every side,
+// with cells no smaller than cell_min and at most table_cap cells (coarser cells if needed).
+__host__ __device__ inline void fit_grid(InstDev& in, int D, const double* lo, const double* hi) {
+  double cs = in.cell_min;
+  for (int it = 0; it < 200; ++it) {
+    unsigned long long cells = 1;
+    for (int a = 0; a < D; ++a) {
+      const double e = (hi[a] - lo[a]) + 4 * cs;
+      unsigned long long n = (unsigned long long)(e / cs) + 1;
+      cells *= n;
+    }
+    if (cells <= in.table_cap) break;
+    cs *= 1.25;
+  }
+  in.cell = cs;
+  in.cell_f = (float)cs;
+  in.inv_cell_f = (float)(1.0 / cs);
+  for (int a = 0; a < 3; ++a) {
+    if (a < D) {
+      in.origin[a] = lo[a] - 2 * cs;
+      in.dims[a] = (uint32_t)(((hi[a] - lo[a]) + 4 * cs) / cs) + 1;
+    } else {
+      in.origin[a] = 0;
+      in.dims[a] = 1;
+    }
+  }
+}
+
+// Clamped cell coordinate of an FP32 offset from the grid origin.
+__host__ __device__ inline int32_t cell_coord(float r, float inv_cell, uint32_t n) {
+  float c = floorf(r * inv_cell);
+  if (!(c >= 0.f)) return 0;  // also catches NaN
+  if (c >= (float)(n - 1)) return (int32_t)(n - 1);
+  return (int32_t)c;
+}
 
 // A wall interaction of one node with one wall side, kept so that the reaction sums can be
 // replayed in the reference's serial node order (contact.h:339, :374, :411-412, :428).
@@ -91,6 +132,7 @@ struct Dev {
   // grains / instances
   GrainDev* grain;
   unsigned long long* bbox;  // [G][2*dim] ordered keys: min..., max...
+  unsigned long long* ibox;  // [I][2*dim] same, per instance (grid refit)
   double* torque_c;          // [G][3] centroid for torque
   InstDev* inst;
   double* reaction;          // [I][2*dim][dim]
@@ -143,29 +185,6 @@ __host__ __device__ inline uint64_t splitmix64(uint64_t x) {
   x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ull;
   x = (x ^ (x >> 27)) * 0x94d049bb133111ebull;
   return x ^ (x >> 31);
-}
-
-__host__ __device__ inline uint32_t morton2(uint32_t x, uint32_t y) {
-  auto spread = [](uint32_t v) {
-    v &= 0xffffu;
-    v = (v | (v << 8)) & 0x00ff00ffu;
-    v = (v | (v << 4)) & 0x0f0f0f0fu;
-    v = (v | (v << 2)) & 0x33333333u;
-    v = (v | (v << 1)) & 0x55555555u;
-    return v;
-  };
-  return spread(x) | (spread(y) << 1);
-}
-__host__ __device__ inline uint32_t morton3(uint32_t x, uint32_t y, uint32_t z) {
-  auto spread = [](uint32_t v) {
-    v &= 0x3ffu;
-    v = (v | (v << 16)) & 0x030000ffu;
-    v = (v | (v << 8)) & 0x0300f00fu;
-    v = (v | (v << 4)) & 0x030c30c3u;
-    v = (v | (v << 2)) & 0x09249249u;
-    return v;
-  };
-  return spread(x) | (spread(y) << 1) | (spread(z) << 2);
 }
 
 }  // namespace pg

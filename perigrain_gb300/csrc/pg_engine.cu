@@ -159,7 +159,7 @@ static int mixed_setup(pg_handle* h, const pg_setup_desc* s) {
   for (uint32_t g = 0; g < P.G; ++g) {
     const InstDev& in = h->inst_host[s->grain_instance[g]];
     for (uint32_t i = s->grain_node_offset[g]; i < s->grain_node_offset[g + 1]; ++i)
-      for (uint32_t c = 0; c < 3; ++c) org[(size_t)i * 3 + c] = in.origin[c];
+      for (uint32_t c = 0; c < 3; ++c) org[(size_t)i * 3 + c] = in.xorigin[c];
   }
   std::vector<float> tmp;
   pack_hl(s->pos, N, D, &org, &tmp);
@@ -281,7 +281,49 @@ static uint32_t next_pow2(uint64_t x) {
   return p;
 }
 
+static int create_impl(const pg_setup_desc* s, const pg_config* cfg_in, pg_handle** out);
+
+// The project's autotuner: every (force-kernel block size, grid cells per node) candidate runs
+// on a trial handle built from the same setup -- 3 warm-up steps, then 12 steps timed with CUDA
+// events on the handle's stream -- and the fastest is kept. The real handle starts from the
+// untouched setup.
 int pg_create(const pg_setup_desc* s, const pg_config* cfg_in, pg_handle** out) {
+  if (!out || !cfg_in) return fail(PG_EINVAL, "null argument");
+  if (!cfg_in->autotune) return create_impl(s, cfg_in, out);
+  const uint32_t blocks[] = {64, 128};
+  const uint32_t cells2[] = {2, 4, 8}, cells3[] = {4, 8, 16};
+  const uint32_t* cells = (s && s->dim == 3) ? cells3 : cells2;
+  double best_ms = 1e300;
+  uint32_t best_b = 128, best_c = cells[1];
+  for (uint32_t b : blocks)
+    for (int ci = 0; ci < 3; ++ci) {
+      pg_config c = *cfg_in;
+      c.autotune = 0;
+      c.block_size = b;
+      c.cells_per_node = cells[ci];
+      c.record_pairs = 0;
+      pg_handle* t = nullptr;
+      int rc = create_impl(s, &c, &t);
+      if (rc) return rc;
+      double ms = 0;
+      rc = pg_step(t, 3);
+      if (!rc) rc = pg_step_timed(t, 12, &ms);
+      pg_destroy(t);
+      if (rc) return rc;
+      if (ms < best_ms) {
+        best_ms = ms;
+        best_b = b;
+        best_c = cells[ci];
+      }
+    }
+  pg_config c = *cfg_in;
+  c.autotune = 0;
+  c.block_size = best_b;
+  c.cells_per_node = best_c;
+  return create_impl(s, &c, out);
+}
+
+static int create_impl(const pg_setup_desc* s, const pg_config* cfg_in, pg_handle** out) {
   if (!out) return fail(PG_EINVAL, "null out");
   *out = nullptr;
   pg_config cfg = *cfg_in;
@@ -306,6 +348,7 @@ int pg_create(const pg_setup_desc* s, const pg_config* cfg_in, pg_handle** out) 
   h->precision = cfg.precision;
   h->next_t = cfg.first_step;
   if (cfg.block_size) h->L.force_block = std::min(128u, std::max(32u, (cfg.block_size / 32) * 32));
+  h->L.cells_per_node = cfg.cells_per_node ? cfg.cells_per_node : ((s->dim == 2) ? 4 : 8);
   Dev& P = h->P;
   P.dim = D;
   P.N = N;
@@ -488,18 +531,27 @@ int pg_create(const pg_setup_desc* s, const pg_config* cfg_in, pg_handle** out) 
     }
     in.node_begin = NONE;
     in.node_end = 0;
+    in.grain_begin = 0;
+    in.grain_end = 0;
   }
   for (uint32_t g = 0; g < G; ++g) {
     InstDev& in = h->inst_host[s->grain_instance[g]];
     in.node_begin = std::min(in.node_begin, s->grain_node_offset[g]);
     in.node_end = std::max(in.node_end, s->grain_node_offset[g + 1]);
+    if (in.grain_end == 0) in.grain_begin = g;
+    in.grain_end = g + 1;
   }
   for (uint32_t k = 0; k < I; ++k) {
     InstDev& in = h->inst_host[k];
     if (in.node_begin == NONE) {  // instance without grains
       in.node_begin = in.node_end = 0;
+      in.grain_begin = in.grain_end = 0;
     }
-    double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+    for (uint32_t a = 0; a < D; ++a) {
+      lo[a] = INFINITY;
+      hi[a] = -INFINITY;
+    }
     for (uint32_t i = in.node_begin; i < in.node_end; ++i)
       for (uint32_t a = 0; a < D; ++a) {
         double x = s->pos[(size_t)i * D + a] + s->disp[(size_t)i * D + a];
@@ -508,26 +560,30 @@ int pg_create(const pg_setup_desc* s, const pg_config* cfg_in, pg_handle** out) 
       }
     double ext = 0;
     for (uint32_t a = 0; a < D; ++a) {
-      if (!std::isfinite(lo[a])) lo[a] = hi[a] = 0;
-      in.origin[a] = 0.5 * (lo[a] + hi[a]);
+      if (!std::isfinite(lo[a]) || !std::isfinite(hi[a])) lo[a] = hi[a] = 0;
+      in.xorigin[a] = 0.5 * (lo[a] + hi[a]);
       ext = std::max(ext, hi[a] - lo[a]);
     }
-    double cell = in.contact_rad * 1.0625;
-    if (!(cell > 0) || !std::isfinite(cell)) cell = std::max(ext, 1e-9) / 64;
-    in.cell = cell;
-    in.cell_f = (float)cell;
-    in.inv_cell_f = (float)(1.0 / cell);
-    in.range_f = (float)(cell * 262144.0);
+    double cmin = in.contact_rad * 1.0625;
+    if (!(cmin > 0) || !std::isfinite(cmin)) cmin = std::max(ext, 1e-9) / 64;
+    in.cell_min = cmin;
+    in.pre_f = (float)cmin;
     const uint32_t nn = in.node_end - in.node_begin;
-    const uint32_t T = next_pow2(std::max<uint64_t>(64, 2ull * nn));
+    in.table_cap = (uint32_t)std::max<uint64_t>(1024, (uint64_t)h->L.cells_per_node * nn);
     in.table_off = (uint32_t)table_total;
-    in.table_mask = T - 1;
-    table_total += T;
+    table_total += in.table_cap;
+    fit_grid(in, (int)D, lo, hi);
   }
   if (table_total >= (1ull << 31)) return fail(PG_EINVAL, "grid table too large");
   P.table_total = (uint32_t)table_total;
   CU(h->dalloc(&P.inst, I));
   CU(cudaMemcpy(P.inst, h->inst_host.data(), I * sizeof(InstDev), cudaMemcpyHostToDevice));
+  CU(h->dalloc(&P.ibox, (size_t)I * 2 * D));
+  {
+    std::vector<unsigned long long> bb((size_t)I * 2 * D);
+    for (size_t i = 0; i < bb.size(); ++i) bb[i] = ((i % (2 * D)) < D) ? ~0ull : 0ull;
+    CU(cudaMemcpy(P.ibox, bb.data(), bb.size() * 8, cudaMemcpyHostToDevice));
+  }
   CU(h->dalloc(&P.reaction, (size_t)I * 2 * D * D));
   CU(cudaMemset(P.reaction, 0, (size_t)I * 2 * D * D * 8));
 
@@ -876,6 +932,13 @@ int pg_get_device_status(pg_handle* h, int32_t* status, uint64_t* too_close) {
   CU(cudaMemcpy(&tc, h->P.too_close, 8, cudaMemcpyDeviceToHost));
   if (status) *status = st;
   if (too_close) *too_close = tc;
+  return PG_OK;
+}
+
+int pg_get_launch_config(pg_handle* h, uint32_t* block_size, uint32_t* cells_per_node) {
+  if (!h) return fail(PG_EINVAL, "null handle");
+  if (block_size) *block_size = h->L.force_block;
+  if (cells_per_node) *cells_per_node = h->L.cells_per_node;
   return PG_OK;
 }
 

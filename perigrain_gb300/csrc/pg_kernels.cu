@@ -57,7 +57,7 @@ __global__ void __launch_bounds__(256) k_predict(const Dev P) {
     for (int c = 0; c < D; ++c) cu[c] = ps[c] + dp[c];
     stv<D>(P.cur, d, cu);
 
-    // grid key from the FP32 offset to the instance origin
+    // grid cell from the FP32 offset to this step's grid origin
     const InstDev& in = P.inst[gr.inst];
     float rf[4] = {0.f, 0.f, 0.f, 0.f};
     int32_t ci[3] = {0, 0, 0};
@@ -65,21 +65,15 @@ __global__ void __launch_bounds__(256) k_predict(const Dev P) {
     for (int c = 0; c < D; ++c) {
       if (!isfinite(cu[c])) ok = false;
       rf[c] = (float)(cu[c] - in.origin[c]);
-      if (!(fabsf(rf[c]) <= in.range_f)) ok = false;
-      ci[c] = (int32_t)floorf(rf[c] * in.inv_cell_f);
+      ci[c] = cell_coord(rf[c], in.inv_cell_f, in.dims[c]);
     }
-    if (!ok) {
-      set_status(P.status, isfinite(cu[0] + cu[1] + (D == 3 ? cu[D - 1] : 0.0)) ? PG_ERANGE : PG_ENAN);
-      for (int c = 0; c < D; ++c) ci[c] = 0;
-    }
+    if (!ok) set_status(P.status, PG_ENAN);
     if constexpr (D == 2) {
       reinterpret_cast<float2*>(P.curf)[d] = make_float2(rf[0], rf[1]);
     } else {
       reinterpret_cast<float4*>(P.curf)[d] = make_float4(rf[0], rf[1], rf[2], 0.f);
     }
-    uint32_t m = (D == 2) ? morton2((uint32_t)ci[0], (uint32_t)ci[1])
-                          : morton3((uint32_t)ci[0], (uint32_t)ci[1], (uint32_t)ci[2]);
-    uint32_t key = in.table_off + (m & in.table_mask);
+    const uint32_t key = in.table_off + ((uint32_t)ci[2] * in.dims[1] + (uint32_t)ci[1]) * in.dims[0] + (uint32_t)ci[0];
     P.cell_key[d] = key;
     P.cell_rank[d] = atomicAdd(&P.cell_count[key], 1u);
     for (int c = 0; c < D; ++c) {
@@ -108,15 +102,21 @@ __global__ void __launch_bounds__(256) k_predict(const Dev P) {
       }
     }
     if (lane == 0) {
+      const uint32_t i0 = P.grain[g0].inst;
       for (int c = 0; c < D; ++c) {
         atomicMin(&P.bbox[(size_t)g0 * 2 * D + c], kmin[c]);
         atomicMax(&P.bbox[(size_t)g0 * 2 * D + D + c], kmax[c]);
+        atomicMin(&P.ibox[(size_t)i0 * 2 * D + c], kmin[c]);
+        atomicMax(&P.ibox[(size_t)i0 * 2 * D + D + c], kmax[c]);
       }
     }
   } else if (act) {
+    const uint32_t i0 = P.grain[g].inst;
     for (int c = 0; c < D; ++c) {
       atomicMin(&P.bbox[(size_t)g * 2 * D + c], kmin[c]);
       atomicMax(&P.bbox[(size_t)g * 2 * D + D + c], kmax[c]);
+      atomicMin(&P.ibox[(size_t)i0 * 2 * D + c], kmin[c]);
+      atomicMax(&P.ibox[(size_t)i0 * 2 * D + D + c], kmax[c]);
     }
   }
 }
@@ -193,50 +193,44 @@ __global__ void __launch_bounds__(128) k_force(const Dev P) {
     float pf[D];
     ldf<D>(P.curf, d, pf);
     int32_t cc[3] = {0, 0, 0};
-    for (int c = 0; c < D; ++c) cc[c] = (int32_t)floorf(pf[c] * in.inv_cell_f);
-    const float thr2 = in.cell_f * in.cell_f;
+    for (int c = 0; c < D; ++c) cc[c] = cell_coord(pf[c], in.inv_cell_f, in.dims[c]);
+    const float thr2 = in.pre_f * in.pre_f;
     unsigned long long keys[MAX_CAND];
     uint32_t idx[MAX_CAND];
     int nc = 0;
-    uint32_t seen[27];
-    int nseen = 0;
-    const int nnb = (D == 2) ? 9 : 27;
-    for (int nb = 0; nb < nnb; ++nb) {
-      int ox = nb % 3 - 1, oy = (nb / 3) % 3 - 1, oz = (D == 3) ? (nb / 9 - 1) : 0;
-      uint32_t m = (D == 2) ? morton2((uint32_t)(cc[0] + ox), (uint32_t)(cc[1] + oy))
-                            : morton3((uint32_t)(cc[0] + ox), (uint32_t)(cc[1] + oy), (uint32_t)(cc[2] + oz));
-      uint32_t bucket = in.table_off + (m & in.table_mask);
-      bool dup = false;
-      for (int s = 0; s < nseen; ++s) dup = dup || (seen[s] == bucket);
-      if (dup) continue;
-      seen[nseen++] = bucket;
-      const uint32_t b0 = P.cell_start[bucket], b1 = P.cell_start[bucket + 1];
-      for (uint32_t b = b0; b < b1; ++b) {
-        const uint32_t q = P.sorted[b];
-        if (q == d) continue;
-        float qf[D];
-        ldf<D>(P.curf, q, qf);
-        float d2 = 0.f;
-        for (int c = 0; c < D; ++c) {
-          float dd = qf[c] - pf[c];
-          d2 += dd * dd;
+    const int z0 = (D == 3) ? max(cc[2] - 1, 0) : 0, z1 = (D == 3) ? min(cc[2] + 1, (int)in.dims[2] - 1) : 0;
+    const int y0 = max(cc[1] - 1, 0), y1 = min(cc[1] + 1, (int)in.dims[1] - 1);
+    const int x0 = max(cc[0] - 1, 0), x1 = min(cc[0] + 1, (int)in.dims[0] - 1);
+    for (int z = z0; z <= z1; ++z)
+      for (int y = y0; y <= y1; ++y) {
+        const uint32_t row = in.table_off + ((uint32_t)z * in.dims[1] + (uint32_t)y) * in.dims[0];
+        const uint32_t b0 = P.cell_start[row + x0], b1 = P.cell_start[row + x1 + 1];
+        for (uint32_t b = b0; b < b1; ++b) {
+          const uint32_t q = P.sorted[b];
+          if (q == d) continue;
+          float qf[D];
+          ldf<D>(P.curf, q, qf);
+          float d2 = 0.f;
+          for (int c = 0; c < D; ++c) {
+            float dd = qf[c] - pf[c];
+            d2 += dd * dd;
+          }
+          if (d2 > thr2) continue;
+          const uint32_t gq = P.node_grain[q];
+          const bool same = (gq == g);
+          if (same ? !selfc : !other) continue;
+          if (P.nl_bdry_only && P.bdry_rank[q] == NONE) continue;
+          if (!same) {
+            double qmn[D], qmx[D];
+            grain_box<D>(P, gq, qmn, qmx);
+            if (!boxes_touch<D>(bmn, bmx, qmn, qmx, in.contact_rad)) continue;
+          }
+          const uint32_t sub = P.nl_bdry_only ? P.bdry_rank[q] : (q - P.grain[gq].node_begin);
+          const unsigned long long key =
+              ((unsigned long long)(same ? 0u : 1u) << 63) | ((unsigned long long)gq << 32) | sub;
+          insert_cand<D>(keys, idx, nc, key, q, P);
         }
-        if (d2 > thr2) continue;
-        const uint32_t gq = P.node_grain[q];
-        const bool same = (gq == g);
-        if (same ? !selfc : !other) continue;
-        if (P.nl_bdry_only && P.bdry_rank[q] == NONE) continue;
-        if (!same) {
-          double qmn[D], qmx[D];
-          grain_box<D>(P, gq, qmn, qmx);
-          if (!boxes_touch<D>(bmn, bmx, qmn, qmx, in.contact_rad)) continue;
-        }
-        const uint32_t sub = P.nl_bdry_only ? P.bdry_rank[q] : (q - P.grain[gq].node_begin);
-        const unsigned long long key =
-            ((unsigned long long)(same ? 0u : 1u) << 63) | ((unsigned long long)gq << 32) | sub;
-        insert_cand<D>(keys, idx, nc, key, q, P);
       }
-    }
     const uint32_t mydeg = P.node_deg[d];
     for (int ci = 0; ci < nc; ++ci) {
       const uint32_t q = idx[ci];

@@ -9,7 +9,8 @@
 namespace pg {
 
 struct LaunchCfg {
-  uint32_t force_block = 128;
+  uint32_t force_block = 128;   // threads per block of the fused force kernel (multiple of 32, <= 128)
+  uint32_t cells_per_node = 4;  // grid capacity per node of an instance
 };
 
 cudaError_t kernels_init();

@@ -22,6 +22,47 @@
 
 namespace pg {
 
+// FP64 <-> FP32 moves done with integer instructions: GB300 executes FP64 arithmetic and the
+// F2F conversions on its narrow FP64 pipe (~1/64 of the FP32 rate), so the per-node hi/lo split
+// and the float->double widening below use bit manipulation on the INT pipe instead.
+//
+// trunc_f32: x truncated to 24 significant bits, as a float and (exactly) as a double. Values
+// below the FP32 normal range become 0 (their size is < 1.2e-38); inf/NaN take the converting
+// path so they propagate.
+__device__ __forceinline__ float trunc_f32(double x, double* as_double) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned int hw = (unsigned int)(b >> 32);
+  const int e = (int)((hw >> 20) & 0x7ffu);
+  if (e < 1023 - 126) {
+    *as_double = 0.0;
+    return 0.f;
+  }
+  if (e > 1023 + 127) {
+    const float f = (float)x;
+    *as_double = (double)f;
+    return f;
+  }
+  *as_double = __longlong_as_double((long long)(b & ~((1ull << 29) - 1)));
+  return __uint_as_float((hw & 0x80000000u) | ((unsigned int)(e - 896) << 23) |
+                         (unsigned int)((b >> 29) & 0x7fffffu));
+}
+// Exact widening of a float; zero and subnormal floats become a signed zero.
+__device__ __forceinline__ double widen(float f) {
+  const unsigned int b = __float_as_uint(f);
+  const unsigned int e = (b >> 23) & 0xffu;
+  const unsigned long long sgn = (unsigned long long)(b & 0x80000000u) << 32;
+  if (e == 0) return __longlong_as_double((long long)sgn);
+  if (e == 0xff) return (double)f;
+  return __longlong_as_double((long long)(sgn | ((unsigned long long)(e + 896) << 52) |
+                                          ((unsigned long long)(b & 0x7fffffu) << 29)));
+}
+// hi/lo pair: x = hi + lo + O(2^-47 |x|)
+__device__ __forceinline__ void split_hl(double x, float* hi, float* lo) {
+  double hd, ld;
+  *hi = trunc_f32(x, &hd);
+  *lo = trunc_f32(x - hd, &ld);
+}
+
 template <int D>
 __device__ __forceinline__ void ld_hl(const float* a, uint32_t i, float (&h)[D], float (&l)[D]) {
   if constexpr (D == 2) {
@@ -44,10 +85,7 @@ __device__ __forceinline__ void ld_hl(const float* a, uint32_t i, float (&h)[D],
 template <int D>
 __device__ __forceinline__ void st_hl(float* a, uint32_t i, const double (&x)[D]) {
   float h[D], l[D];
-  for (int c = 0; c < D; ++c) {
-    h[c] = (float)x[c];
-    l[c] = (float)(x[c] - (double)h[c]);
-  }
+  for (int c = 0; c < D; ++c) split_hl(x[c], &h[c], &l[c]);
   if constexpr (D == 2) {
     reinterpret_cast<float4*>(a)[i] = make_float4(h[0], h[1], l[0], l[1]);
   } else {
@@ -106,11 +144,17 @@ __global__ void __launch_bounds__(256) k_predict_mx(const Dev P) {
       wrote = true;
     }
     if (gr.flags & GF_MOVABLE) {
-      double v[D];
+      // the increment dt*v + (dt*dt/2)*a is formed in FP32 (relative error ~1e-7 of a step's
+      // motion); the accumulation into disp stays FP64
+      double v[D], vd;
       float a[D];
       ldv<D>(P.vel_in, d, v);
       ldvf<D>(P.acc_f, d, a);
-      for (int c = 0; c < D; ++c) dp[c] = dp[c] + fma(P.dt, v[c], P.hdt2 * (double)a[c]);
+      const float dtf = (float)P.dt, hdt2f = (float)P.hdt2;
+      for (int c = 0; c < D; ++c) {
+        const float vf = trunc_f32(v[c], &vd);
+        dp[c] = dp[c] + widen(fmaf(dtf, vf, hdt2f * a[c]));
+      }
       wrote = true;
     }
     if (wrote) {
@@ -125,26 +169,28 @@ __global__ void __launch_bounds__(256) k_predict_mx(const Dev P) {
     float rf[4] = {0.f, 0.f, 0.f, 0.f};
     int32_t ci[3] = {0, 0, 0};
     bool ok = true;
+    float rh[D], rl[D];
     for (int c = 0; c < D; ++c) {
-      if (!isfinite(cu[c])) ok = false;
+      if (((__double_as_longlong(cu[c]) >> 52) & 0x7ff) == 0x7ff) ok = false;  // inf or NaN
       rel[c] = cu[c] - in.origin[c];
-      rf[c] = (float)rel[c];
-      if (!(fabsf(rf[c]) <= in.range_f)) ok = false;
-      ci[c] = (int32_t)floorf(rf[c] * in.inv_cell_f);
+      split_hl(rel[c], &rh[c], &rl[c]);
+      rf[c] = rh[c];
+      ci[c] = cell_coord(rf[c], in.inv_cell_f, in.dims[c]);
     }
-    if (!ok) {
-      set_status(P.status, isfinite(cu[0] + cu[1] + (D == 3 ? cu[D - 1] : 0.0)) ? PG_ERANGE : PG_ENAN);
-      for (int c = 0; c < D; ++c) ci[c] = 0;
+    if (!ok) set_status(P.status, PG_ENAN);
+    if constexpr (D == 2) {
+      reinterpret_cast<float4*>(P.cur_hl)[d] = make_float4(rh[0], rh[1], rl[0], rl[1]);
+    } else {
+      float4* q = reinterpret_cast<float4*>(P.cur_hl) + 2ull * d;
+      q[0] = make_float4(rh[0], rh[1], rh[2], 0.f);
+      q[1] = make_float4(rl[0], rl[1], rl[2], 0.f);
     }
-    st_hl<D>(P.cur_hl, d, rel);
     if constexpr (D == 2) {
       reinterpret_cast<float2*>(P.curf)[d] = make_float2(rf[0], rf[1]);
     } else {
       reinterpret_cast<float4*>(P.curf)[d] = make_float4(rf[0], rf[1], rf[2], 0.f);
     }
-    uint32_t m = (D == 2) ? morton2((uint32_t)ci[0], (uint32_t)ci[1])
-                          : morton3((uint32_t)ci[0], (uint32_t)ci[1], (uint32_t)ci[2]);
-    uint32_t key = in.table_off + (m & in.table_mask);
+    const uint32_t key = in.table_off + ((uint32_t)ci[2] * in.dims[1] + (uint32_t)ci[1]) * in.dims[0] + (uint32_t)ci[0];
     P.cell_key[d] = key;
     P.cell_rank[d] = atomicAdd(&P.cell_count[key], 1u);
     for (int c = 0; c < D; ++c) {
@@ -172,17 +218,45 @@ __global__ void __launch_bounds__(256) k_predict_mx(const Dev P) {
       }
     }
     if (lane == 0) {
+      const uint32_t i0 = P.grain[g0].inst;
       for (int c = 0; c < D; ++c) {
         atomicMin(&P.bbox[(size_t)g0 * 2 * D + c], kmin[c]);
         atomicMax(&P.bbox[(size_t)g0 * 2 * D + D + c], kmax[c]);
+        atomicMin(&P.ibox[(size_t)i0 * 2 * D + c], kmin[c]);
+        atomicMax(&P.ibox[(size_t)i0 * 2 * D + D + c], kmax[c]);
       }
     }
   } else if (act) {
+    const uint32_t i0 = P.grain[g].inst;
     for (int c = 0; c < D; ++c) {
       atomicMin(&P.bbox[(size_t)g * 2 * D + c], kmin[c]);
       atomicMax(&P.bbox[(size_t)g * 2 * D + D + c], kmax[c]);
+      atomicMin(&P.ibox[(size_t)i0 * 2 * D + c], kmin[c]);
+      atomicMax(&P.ibox[(size_t)i0 * 2 * D + D + c], kmax[c]);
     }
   }
+}
+
+// One bond: stretch s = (2 xi.eta + eta.eta) / (|xi| (|xi+eta| + |xi|)), force density
+// cnot * s * vol_j * (xi+eta)/|xi+eta| added to f when `use`. cv = cnot * vol_j.
+template <int D>
+__device__ __forceinline__ void bond_term(const float (&dh)[D], const float (&dl)[D], const float (&xh)[D],
+                                          const float (&xl)[D], const float (&jdh)[D], const float (&jdl)[D],
+                                          const float (&jxh)[D], const float (&jxl)[D], float cv, bool use,
+                                          float (&f)[D], float* str_out) {
+  float xi[D], et[D], y[D];
+  for (int c = 0; c < D; ++c) {
+    xi[c] = (jxh[c] - xh[c]) + (jxl[c] - xl[c]);
+    et[c] = (jdh[c] - dh[c]) + (jdl[c] - dl[c]);
+    y[c] = xi[c] + et[c];
+  }
+  const float xx = dotf<D>(xi, xi), yy = dotf<D>(y, y);
+  const float ixn = rsqrtf(xx), iyn = rsqrtf(yy);
+  const float num = fmaf(2.f, dotf<D>(xi, et), dotf<D>(et, et));
+  const float str = __fdividef(num * ixn, fmaf(yy, iyn, xx * ixn));
+  const float sc = use ? cv * str * iyn : 0.f;
+  for (int c = 0; c < D; ++c) f[c] = fmaf(sc, y[c], f[c]);
+  *str_out = str;
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -216,35 +290,39 @@ __global__ void __launch_bounds__(128) k_force_mx(const Dev P) {
       ld_hl<D>(P.disp_hl, d, dh, dl);
       ld_hl<D>(P.xpos_hl, d, xh, xl);
     }
-    for (uint32_t k = 0; k < cdeg; ++k) {
-      const uint32_t word = P.alive[w0 + k];
-      bool bit = (word >> lane) & 1u;
-      if (mov && bit) {
-        const uint32_t s = slot0 + 32u * k;
-        const uint32_t j = P.bcol[s];
-        float jdh[D], jdl[D], jxh[D], jxl[D];
-        ld_hl<D>(P.disp_hl, j, jdh, jdl);
-        ld_hl<D>(P.xpos_hl, j, jxh, jxl);
-        const float vj = P.vol_f[j];
-        float xi[D], et[D], y[D];
-        for (int c = 0; c < D; ++c) {
-          xi[c] = (jxh[c] - xh[c]) + (jxl[c] - xl[c]);
-          et[c] = (jdh[c] - dh[c]) + (jdl[c] - dl[c]);
-          y[c] = xi[c] + et[c];
-        }
-        const float xn = sqrtf(dotf<D>(xi, xi));
-        const float yn = sqrtf(dotf<D>(y, y));
-        const float num = fmaf(2.f, dotf<D>(xi, et), dotf<D>(et, et));
-        const float str = num / (xn * (yn + xn));
-        const float sc = (cnot * str * vj) / yn;
-        for (int c = 0; c < D; ++c) f[c] = fmaf(sc, y[c], f[c]);
-        if (brk && str > snot) {
-          bit = false;
-          P.break_step[s] = t;
-        }
+    // two bonds per iteration: both neighbour gathers are issued before either is used
+    for (uint32_t k = 0; k < cdeg; k += 2) {
+      const bool two = (k + 1) < cdeg;
+      const uint32_t wa = P.alive[w0 + k];
+      const uint32_t wb = two ? P.alive[w0 + k + 1] : 0u;
+      bool ba = (wa >> lane) & 1u, bb = (wb >> lane) & 1u;
+      const bool ua = mov && ba, ub = mov && bb;
+      const uint32_t sa = slot0 + 32u * k, sb = sa + 32u;
+      const uint32_t ja = ua ? P.bcol[sa] : d;
+      const uint32_t jb = ub ? P.bcol[sb] : d;
+      float adh[D], adl[D], axh[D], axl[D], bdh[D], bdl[D], bxh[D], bxl[D];
+      ld_hl<D>(P.disp_hl, ja, adh, adl);
+      ld_hl<D>(P.xpos_hl, ja, axh, axl);
+      ld_hl<D>(P.disp_hl, jb, bdh, bdl);
+      ld_hl<D>(P.xpos_hl, jb, bxh, bxl);
+      const float va = P.vol_f[ja], vb = P.vol_f[jb];
+      float stra, strb;
+      bond_term<D>(dh, dl, xh, xl, adh, adl, axh, axl, cnot * va, ua, f, &stra);
+      bond_term<D>(dh, dl, xh, xl, bdh, bdl, bxh, bxl, cnot * vb, ub, f, &strb);
+      if (brk && ua && stra > snot) {
+        ba = false;
+        P.break_step[sa] = t;
       }
-      const uint32_t nw = __ballot_sync(0xffffffffu, bit);
-      if (lane == 0 && nw != word) P.alive[w0 + k] = nw;
+      if (brk && ub && strb > snot) {
+        bb = false;
+        P.break_step[sb] = t;
+      }
+      const uint32_t na = __ballot_sync(0xffffffffu, ba);
+      const uint32_t nb = __ballot_sync(0xffffffffu, bb);
+      if (lane == 0) {
+        if (na != wa) P.alive[w0 + k] = na;
+        if (two && nb != wb) P.alive[w0 + k + 1] = nb;
+      }
     }
   }
   __syncwarp();
@@ -263,78 +341,84 @@ __global__ void __launch_bounds__(128) k_force_mx(const Dev P) {
     float ph[D], pl[D];
     ld_hl<D>(P.cur_hl, d, ph, pl);
     int32_t cc[3] = {0, 0, 0};
-    for (int c = 0; c < D; ++c) cc[c] = (int32_t)floorf(ph[c] * in.inv_cell_f);
-    const float thr2 = in.cell_f * in.cell_f;
+    for (int c = 0; c < D; ++c) cc[c] = cell_coord(ph[c], in.inv_cell_f, in.dims[c]);
+    const float thr2 = in.pre_f * in.pre_f;
     unsigned long long keys[MAX_CAND];
     uint32_t idx[MAX_CAND];
     int nc = 0;
-    uint32_t seen[27];
-    int nseen = 0;
-    const int nnb = (D == 2) ? 9 : 27;
-    for (int nb = 0; nb < nnb; ++nb) {
-      int ox = nb % 3 - 1, oy = (nb / 3) % 3 - 1, oz = (D == 3) ? (nb / 9 - 1) : 0;
-      uint32_t m = (D == 2) ? morton2((uint32_t)(cc[0] + ox), (uint32_t)(cc[1] + oy))
-                            : morton3((uint32_t)(cc[0] + ox), (uint32_t)(cc[1] + oy), (uint32_t)(cc[2] + oz));
-      uint32_t bucket = in.table_off + (m & in.table_mask);
-      bool dup = false;
-      for (int s = 0; s < nseen; ++s) dup = dup || (seen[s] == bucket);
-      if (dup) continue;
-      seen[nseen++] = bucket;
-      const uint32_t b0 = P.cell_start[bucket], b1 = P.cell_start[bucket + 1];
-      for (uint32_t b = b0; b < b1; ++b) {
-        const uint32_t q = P.sorted[b];
-        if (q == d) continue;
-        float qf[D];
-        ldf<D>(P.curf, q, qf);
-        float d2 = 0.f;
-        for (int c = 0; c < D; ++c) {
-          float dd = qf[c] - ph[c];
-          d2 = fmaf(dd, dd, d2);
+    const int z0 = (D == 3) ? max(cc[2] - 1, 0) : 0, z1 = (D == 3) ? min(cc[2] + 1, (int)in.dims[2] - 1) : 0;
+    const int y0 = max(cc[1] - 1, 0), y1 = min(cc[1] + 1, (int)in.dims[1] - 1);
+    const int x0 = max(cc[0] - 1, 0), x1 = min(cc[0] + 1, (int)in.dims[0] - 1);
+    for (int z = z0; z <= z1; ++z)
+      for (int y = y0; y <= y1; ++y) {
+        const uint32_t row = in.table_off + ((uint32_t)z * in.dims[1] + (uint32_t)y) * in.dims[0];
+        const uint32_t b0 = P.cell_start[row + x0], b1 = P.cell_start[row + x1 + 1];
+        for (uint32_t b = b0; b < b1; ++b) {
+          const uint32_t q = P.sorted[b];
+          if (q == d) continue;
+          float qf[D];
+          ldf<D>(P.curf, q, qf);
+          float d2 = 0.f;
+          for (int c = 0; c < D; ++c) {
+            float dd = qf[c] - ph[c];
+            d2 = fmaf(dd, dd, d2);
+          }
+          if (d2 > thr2) continue;
+          const uint32_t gq = P.node_grain[q];
+          const bool same = (gq == g);
+          if (same ? !selfc : !other) continue;
+          if (P.nl_bdry_only && P.bdry_rank[q] == NONE) continue;
+          if (!same) {
+            double qmn[D], qmx[D];
+            grain_box<D>(P, gq, qmn, qmx);
+            if (!boxes_touch<D>(bmn, bmx, qmn, qmx, in.contact_rad)) continue;
+          }
+          const uint32_t sub = P.nl_bdry_only ? P.bdry_rank[q] : (q - P.grain[gq].node_begin);
+          const unsigned long long key =
+              ((unsigned long long)(same ? 0u : 1u) << 63) | ((unsigned long long)gq << 32) | sub;
+          insert_cand<D>(keys, idx, nc, key, q, P);
         }
-        if (d2 > thr2) continue;
-        const uint32_t gq = P.node_grain[q];
-        const bool same = (gq == g);
-        if (same ? !selfc : !other) continue;
-        if (P.nl_bdry_only && P.bdry_rank[q] == NONE) continue;
-        if (!same) {
-          double qmn[D], qmx[D];
-          grain_box<D>(P, gq, qmn, qmx);
-          if (!boxes_touch<D>(bmn, bmx, qmn, qmx, in.contact_rad)) continue;
-        }
-        const uint32_t sub = P.nl_bdry_only ? P.bdry_rank[q] : (q - P.grain[gq].node_begin);
-        const unsigned long long key =
-            ((unsigned long long)(same ? 0u : 1u) << 63) | ((unsigned long long)gq << 32) | sub;
-        insert_cand<D>(keys, idx, nc, key, q, P);
       }
-    }
     const uint32_t mydeg = P.node_deg[d];
     const float Rc0 = (float)in.contact_rad, Kn0 = (float)in.normal_stiffness;
     const float mu = (float)in.friction_coefficient, zeta = (float)in.damping_ratio;
     const float rho = (float)gr.rho, dtf = (float)P.dt;
+    double xp64[D];
+    if (nc) ldv<D>(P.cur, d, xp64);
     for (int ci = 0; ci < nc; ++ci) {
       const uint32_t q = idx[ci];
       const bool same = (keys[ci] >> 63) == 0;
-      float qh[D], ql[D], dir[D];
-      ld_hl<D>(P.cur_hl, q, qh, ql);
-      for (int c = 0; c < D; ++c) dir[c] = (qh[c] - ph[c]) + (ql[c] - pl[c]);
-      const float dn = sqrtf(dotf<D>(dir, dir));
-      float Rc = Rc0, Kn = Kn0;
+      // The contact decision |x_q - x_p| <= R_c' is made with the reference's FP64 arithmetic:
+      // contact damping switches on at full strength at that boundary, so a decision flipped by
+      // FP32 rounding would kick a node by metres per second.
+      double xq64[D], dir64[D];
+      ldv<D>(P.cur, q, xq64);
+      for (int c = 0; c < D; ++c) dir64[c] = xq64[c] - xp64[c];
+      double n2 = dir64[0] * dir64[0];
+      for (int c = 1; c < D; ++c) n2 = n2 + dir64[c] * dir64[c];
+      const double dn64 = sqrt(n2);
+      double Rc64 = in.contact_rad;
+      float Kn = Kn0;
       if (same) {
         bool bonded = false;
         for (uint32_t k = 0; k < mydeg && !bonded; ++k) {
           if (((P.alive[w0 + k] >> lane) & 1u) && P.bcol[slot0 + 32u * k] == q) bonded = true;
         }
         if (bonded) continue;
-        double pp[D], pq[D];
+        double pp[D], pq[D], r[D];
         ldv<D>(P.pos, d, pp);
         ldv<D>(P.pos, q, pq);
-        float r[D];
-        for (int c = 0; c < D; ++c) r[c] = (float)(pp[c] - pq[c]);
-        const float ref = sqrtf(dotf<D>(r, r));
-        Rc = ref < Rc0 ? ref : Rc0;
-        Kn = (float)gr.cnot / Rc;
+        for (int c = 0; c < D; ++c) r[c] = pp[c] - pq[c];
+        double r2 = r[0] * r[0];
+        for (int c = 1; c < D; ++c) r2 = r2 + r[c] * r[c];
+        const double ref = sqrt(r2);
+        Rc64 = ref < in.contact_rad ? ref : in.contact_rad;
+        Kn = (float)(gr.cnot / Rc64);
       }
-      if (!(dn <= Rc)) continue;
+      if (!(dn64 <= Rc64)) continue;
+      const float Rc = (float)Rc64, dn = (float)dn64;
+      float dir[D];
+      for (int c = 0; c < D; ++c) dir[c] = (float)dir64[c];
       if (P.record_pairs) {
         my_pairs += 1;
         my_hash += splitmix64(((unsigned long long)d << 32) | q);
@@ -491,10 +575,10 @@ __global__ void __launch_bounds__(128) k_force_mx(const Dev P) {
       float ao[D], a[D];
       double v[D];
       ldvf<D>(P.acc_f, d, ao);
-      const float orho = (float)gr.one_over_rho;
+      const float orho = (float)gr.one_over_rho, hdt = (float)P.half_dt;
       for (int c = 0; c < D; ++c) {
         a[c] = orho * f[c];
-        v[c] = vpd[c] + ((double)ao[c] + (double)a[c]) * P.half_dt;
+        v[c] = vpd[c] + widen((ao[c] + a[c]) * hdt);  // FP64 accumulation of an FP32 increment
       }
       if (P.clamped[d]) {
         for (int c = 0; c < D; ++c) {

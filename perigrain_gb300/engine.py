@@ -17,7 +17,8 @@ from . import _native as N
 class Simulation:
     def __init__(self, setup, dt, enable_fracture=1, nl_bdry_only=0, allow_damping=1, allow_friction=1,
                  self_contact=1, enable_torque=0, gradient_extforce=0, extforce_maxstep=0, precision="fp64",
-                 record_pairs=False, pair_log_capacity=1024, first_step=1, max_contacts=48, block_size=0):
+                 record_pairs=False, pair_log_capacity=1024, first_step=1, max_contacts=48, block_size=0,
+                 autotune=False, cells_per_node=0):
         L = N.lib()
         self.setup = setup
         self.dim = setup.dim
@@ -38,6 +39,8 @@ class Simulation:
         cfg.first_step = int(first_step)
         cfg.max_contacts = int(max_contacts)
         cfg.block_size = int(block_size)
+        cfg.autotune = int(bool(autotune))
+        cfg.cells_per_node = int(cells_per_node)
         self.cfg = cfg
         self._desc = setup.desc()
         h = C.c_void_p()
@@ -131,6 +134,11 @@ class Simulation:
         n = C.c_uint64()
         N.check(N.lib().pg_get_launch_count(self.h, C.byref(n)))
         return n.value
+
+    def launch_config(self):
+        b, c = C.c_uint32(), C.c_uint32()
+        N.check(N.lib().pg_get_launch_config(self.h, C.byref(b), C.byref(c)))
+        return dict(block_size=b.value, cells_per_node=c.value)
 
     def set_timing(self, on):
         N.check(N.lib().pg_set_timing(self.h, int(bool(on))))
