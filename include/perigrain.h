@@ -188,6 +188,20 @@ int pg_get_launch_count(pg_handle* h, uint64_t* launches);
 int pg_set_timing(pg_handle* h, int32_t enable);
 int pg_get_kernel_times(pg_handle* h, double* force_ms, double* total_ms, uint64_t* force_launches);
 
+/* ---- setup helpers -------------------------------------------------------------------------- */
+/* Bond list of one grain on the GPU: every node pair (i, j), i < j, with
+ * sqrt(sum_c (p_j[c] - p_i[c])^2) <= delta, rows in lexicographic order -- the Connectivity the
+ * reference's setup writes (exp_dict.py:171-222: itertools.combinations + single_bond, which
+ * compares the same FP64 distance). pos: device pointer, n x dim doubles; pairs: device pointer,
+ * capacity x 2 uint32. *n_pairs receives the number of pairs (also when it exceeds capacity, then
+ * PG_ECAPACITY and the first `capacity` rows are written). Temporary device memory is allocated
+ * and freed inside the call. Runs on `stream` (a cudaStream_t, NULL for the default stream) and
+ * returns after it completes. pg_bond_last_error() describes a failure. */
+int pg_build_bonds(const double* pos, uint32_t n, uint32_t dim, double delta, uint32_t* pairs,
+                   uint64_t capacity, uint64_t* n_pairs, void* stream);
+const char* pg_bond_last_error(void);
+
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,31 @@
+// Internal interface of the GPU bond-list builder (pg_bonds.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+
+namespace pg {
+
+// Device scratch of one bond build. `cells` is the capacity of the cell arrays.
+struct BondScratch {
+  unsigned long long* box;  // [6] ordered-key bounding box
+  uint32_t* cell_count;     // [cells]
+  uint32_t* cell_start;     // [cells + 1]
+  uint32_t* key;            // [n]
+  uint32_t* rank;           // [n]
+  uint32_t* sorted;         // [n]
+  uint32_t* pcount;         // [n]
+  uint32_t* poff;           // [n + 1]
+  uint32_t* tile_sum;       // [bond_scan_tiles(max(cells, n))]
+  uint32_t* done;           // [1]
+  int32_t* error;           // [1]
+  uint32_t cells;
+};
+
+uint32_t bond_grid_cells(uint32_t n);
+uint32_t bond_scan_tiles(uint32_t len);
+int run_bond_build(const double* pos, uint32_t n, uint32_t dim, double delta, uint32_t* pairs, uint64_t capacity,
+                   uint64_t* n_pairs, cudaStream_t st, const BondScratch& S, std::string* err);
+
+}  // namespace pg
