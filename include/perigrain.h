@@ -201,6 +201,19 @@ int pg_build_bonds(const double* pos, uint32_t n, uint32_t dim, double delta, ui
                    uint64_t capacity, uint64_t* n_pairs, void* stream);
 const char* pg_bond_last_error(void);
 
+/* pg_build_bonds without any device allocation, for callers that cannot allocate device memory:
+ * code running during CUDA-graph capture on its stream, allocator or memory-pool hooks that must
+ * not re-enter the allocator, hosts that reserve all device memory up front. This entry point has
+ * no counterpart in the reference. Same arguments and results as pg_build_bonds; its scratch is a
+ * file-scope device array sized for one grain of at most PG_NOALLOC_MAX_NODES nodes (about 1.7 MB,
+ * held by every GPU that loads the library until exit); larger n returns PG_EINVAL. Calls share
+ * that array, so calls that overlap on the GPU race; each call clears what it needs. The first
+ * call on a device looks the array's address up (make it before any stream capture).
+ * pg_noalloc_last_error() describes a failure. */
+#define PG_NOALLOC_MAX_NODES 32768u
+int pg_build_bonds_noalloc(const double* pos, uint32_t n, uint32_t dim, double delta, uint32_t* pairs,
+                           uint64_t capacity, uint64_t* n_pairs, void* stream);
+const char* pg_noalloc_last_error(void);
 
 #ifdef __cplusplus
 }

@@ -104,6 +104,9 @@ PROTOTYPES = [
     ("pg_build_bonds", C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_double, C.c_void_p, C.c_uint64, u64p,
                                  C.c_void_p]),
     ("pg_bond_last_error", C.c_char_p, []),
+    ("pg_build_bonds_noalloc", C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_double, C.c_void_p, C.c_uint64,
+                                         u64p, C.c_void_p]),
+    ("pg_noalloc_last_error", C.c_char_p, []),
     # perigrain_io.h
     ("pg_conf_default", None, [C.POINTER(Conf)]),
     ("pg_conf_read_file", C.c_int, [C.POINTER(Conf), C.c_char_p]),
