@@ -35,9 +35,9 @@ METRIC = "node-steps/s"
 #   FP64:  per node  reads disp, xpos, cur, vel, acc, extforce (8*dim B each), vol (8), grain id
 #          and degree (4 + 4); writes acc, vel, force (8*dim each) -> 72*dim + 16 B
 #          per bond  neighbour id (4 B) + xi_norm (8 B) + one alive bit          -> 12.125 B
-#   mixed: per node  reads FP32 hi/lo disp, xpos, cur (8*dim each), FP64 vel (8*dim), FP32 acc and
-#          extforce (4*dim each), grain id (4); writes FP32 acc (4*dim), FP64 vel (8*dim),
-#          FP32 force (4*dim)                                                    -> 56*dim + 4 B
+#   mixed: per node  reads the FP32 hi/lo record of disp and xpos (16*dim), hi/lo cur (8*dim), FP64
+#          vel (8*dim), FP32 acc and extforce (4*dim each), grain id (4); writes FP32 acc (4*dim),
+#          FP64 vel (8*dim), FP32 force (4*dim)                                  -> 56*dim + 4 B
 #          per bond  neighbour id (4 B) + one alive bit                          -> 4.125 B
 
 

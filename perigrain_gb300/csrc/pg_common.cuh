@@ -60,8 +60,8 @@ __device__ __forceinline__ void set_status(int32_t* st, int32_t code) { atomicCA
 // ---------------------------------------------------------------------------------------------
 // Exclusive scan of cell_count -> cell_start (reduce-then-scan, last block scans tile sums).
 // ---------------------------------------------------------------------------------------------
-constexpr int SCAN_THREADS = 1024;
-constexpr int SCAN_PER = 4;
+constexpr int SCAN_THREADS = 256;
+constexpr int SCAN_PER = 16;  // four uint4 loads per thread
 constexpr int SCAN_TILE = SCAN_THREADS * SCAN_PER;
 
 __device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* warp_sums, uint32_t* total) {
@@ -95,8 +95,10 @@ static __global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(const Dev P
   const uint32_t base = tile * SCAN_TILE + threadIdx.x * SCAN_PER;
   uint32_t s = 0;
   if (base + SCAN_PER <= P.table_total) {
-    const uint4 v = *reinterpret_cast<const uint4*>(P.cell_count + base);
-    s = v.x + v.y + v.z + v.w;
+    const uint4* q = reinterpret_cast<const uint4*>(P.cell_count + base);
+    uint4 v[SCAN_PER / 4];
+    for (int k = 0; k < SCAN_PER / 4; ++k) v[k] = q[k];
+    for (int k = 0; k < SCAN_PER / 4; ++k) s += v[k].x + v[k].y + v[k].z + v[k].w;
   } else {
     for (int k = 0; k < SCAN_PER; ++k) {
       uint32_t i = base + k;
@@ -138,11 +140,14 @@ static __global__ void __launch_bounds__(SCAN_THREADS) k_scan_final(const Dev P)
   uint32_t s = 0;
   const bool full = base + SCAN_PER <= P.table_total;
   if (full) {
-    const uint4 q = *reinterpret_cast<const uint4*>(P.cell_count + base);
-    v[0] = q.x;
-    v[1] = q.y;
-    v[2] = q.z;
-    v[3] = q.w;
+    const uint4* q4 = reinterpret_cast<const uint4*>(P.cell_count + base);
+    for (int k = 0; k < SCAN_PER / 4; ++k) {
+      const uint4 q = q4[k];
+      v[4 * k] = q.x;
+      v[4 * k + 1] = q.y;
+      v[4 * k + 2] = q.z;
+      v[4 * k + 3] = q.w;
+    }
   } else {
     for (int k = 0; k < SCAN_PER; ++k) {
       uint32_t i = base + k;
@@ -158,8 +163,10 @@ static __global__ void __launch_bounds__(SCAN_THREADS) k_scan_final(const Dev P)
   }
   if (full) {
     // cell_start has table_total + 1 entries, so base need not be 16-byte aligned: plain stores
-    for (int k = 0; k < SCAN_PER; ++k) P.cell_start[base + k] = st[k];
-    *reinterpret_cast<uint4*>(P.cell_count + base) = make_uint4(0, 0, 0, 0);  // next step's counts
+    uint4* s4 = reinterpret_cast<uint4*>(P.cell_start + base);  // base is a multiple of 16 entries
+    for (int k = 0; k < SCAN_PER / 4; ++k) s4[k] = make_uint4(st[4 * k], st[4 * k + 1], st[4 * k + 2], st[4 * k + 3]);
+    uint4* z4 = reinterpret_cast<uint4*>(P.cell_count + base);
+    for (int k = 0; k < SCAN_PER / 4; ++k) z4[k] = make_uint4(0, 0, 0, 0);  // next step's counts
   } else {
     for (int k = 0; k < SCAN_PER; ++k) {
       uint32_t i = base + k;
@@ -340,15 +347,23 @@ static __global__ void __launch_bounds__(FINAL_THREADS) k_finalize(const Dev P) 
     const int s = p % NS;
     in->wall[s] = in->wall[s] + in->wall_speed[s] * P.dt;
   }
-  // refit every instance's grid to this step's bounding box for the next step
+  // refit every instance's grid to this step's bounding box for the next step: grain boxes are
+  // folded into per-instance boxes (one atomic per grain and bound), then one thread per instance
+  for (uint32_t g = tid; g < P.G; g += blockDim.x) {
+    const uint32_t k = P.grain[g].inst;
+    for (int c = 0; c < D; ++c) {
+      atomicMin(&P.ibox[(size_t)k * NS + c], P.bbox[(size_t)g * NS + c]);
+      atomicMax(&P.ibox[(size_t)k * NS + D + c], P.bbox[(size_t)g * NS + D + c]);
+    }
+  }
+  __syncthreads();
   for (uint32_t k = tid; k < P.I; k += blockDim.x) {
     InstDev* in = &P.inst[k];
-    if (in->grain_end <= in->grain_begin) continue;
     double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
-    bool ok = true;
+    bool ok = in->grain_end > in->grain_begin;
     for (int c = 0; c < D; ++c) {
-      lo[c] = ordered_to_dbl(P.ibox[(size_t)k * NS + c]);
-      hi[c] = ordered_to_dbl(P.ibox[(size_t)k * NS + D + c]);
+      lo[c] = ordered_to_dbl(__ldcg(&P.ibox[(size_t)k * NS + c]));  // atomics live in L2
+      hi[c] = ordered_to_dbl(__ldcg(&P.ibox[(size_t)k * NS + D + c]));
       ok = ok && isfinite(lo[c]) && isfinite(hi[c]);
       P.ibox[(size_t)k * NS + c] = ~0ull;
       P.ibox[(size_t)k * NS + D + c] = 0ull;

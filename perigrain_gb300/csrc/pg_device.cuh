@@ -64,28 +64,28 @@ struct InstDev {
 // Fit the grid of one instance to the node bounding box [lo, hi] plus two cells on every side,
 // with cells no smaller than cell_min and at most table_cap cells (coarser cells if needed).
 __host__ __device__ inline void fit_grid(InstDev& in, int D, const double* lo, const double* hi) {
-  double cs = in.cell_min;
+  // cell counts in FP32 (the grid only has to cover the box; the exact origin stays FP64) -- this
+  // runs once per instance per step inside a single block, where FP64 division would be slow
+  float cs = (float)in.cell_min;
+  float ext[3] = {0.f, 0.f, 0.f};
+  for (int a = 0; a < D; ++a) ext[a] = (float)(hi[a] - lo[a]);
+  uint32_t n[3] = {1, 1, 1};
   for (int it = 0; it < 200; ++it) {
+    const float inv = 1.f / cs;
     unsigned long long cells = 1;
     for (int a = 0; a < D; ++a) {
-      const double e = (hi[a] - lo[a]) + 4 * cs;
-      unsigned long long n = (unsigned long long)(e / cs) + 1;
-      cells *= n;
+      n[a] = (uint32_t)(ext[a] * inv) + 5u;  // + two cells of margin on each side + rounding
+      cells *= n[a];
     }
     if (cells <= in.table_cap) break;
-    cs *= 1.25;
+    cs *= 1.25f;
   }
-  in.cell = cs;
-  in.cell_f = (float)cs;
-  in.inv_cell_f = (float)(1.0 / cs);
+  in.cell = (double)cs;
+  in.cell_f = cs;
+  in.inv_cell_f = 1.f / cs;
   for (int a = 0; a < 3; ++a) {
-    if (a < D) {
-      in.origin[a] = lo[a] - 2 * cs;
-      in.dims[a] = (uint32_t)(((hi[a] - lo[a]) + 4 * cs) / cs) + 1;
-    } else {
-      in.origin[a] = 0;
-      in.dims[a] = 1;
-    }
+    in.origin[a] = a < D ? lo[a] - 2.0 * (double)cs : 0.0;
+    in.dims[a] = a < D ? n[a] : 1u;
   }
 }
 
@@ -132,7 +132,7 @@ struct Dev {
   // grains / instances
   GrainDev* grain;
   unsigned long long* bbox;  // [G][2*dim] ordered keys: min..., max...
-  unsigned long long* ibox;  // [I][2*dim] same, per instance (grid refit)
+  unsigned long long* ibox;  // [I][2*dim] same, per instance (grid refit in k_finalize)
   double* torque_c;          // [G][3] centroid for torque
   InstDev* inst;
   double* reaction;          // [I][2*dim][dim]
@@ -153,12 +153,31 @@ struct Dev {
   int32_t enable_torque, gradient_extforce, record_pairs;
   uint32_t extforce_maxstep;
   uint32_t max_cand;
-  // mixed precision (PG_MIXED): FP32 hi/lo pairs (hi = (float)x, lo = (float)(x - hi)) of the FP64
-  // displacement, of the bond reference positions and of CurrPos (both relative to the instance
-  // origin), 2*SF floats per node; FP32 acceleration, force, external force and volume.
-  float *disp_hl, *xpos_hl, *cur_hl;
+  // mixed precision (PG_MIXED): FP32 hi/lo pairs (x = hi + lo to ~2^-47 |x|). `bref` interleaves,
+  // per node, the pair of the FP64 displacement and the pair of the bond reference position
+  // (relative to the instance's fixed origin) -- 4*SF floats, one 32-byte sector in 2D -- so a bond
+  // gathers its neighbour's data from one sector. `cur_hl` holds CurrPos relative to the grid
+  // origin (2*SF floats). FP32 acceleration, force, external force and volume.
+  float *bref, *cur_hl;
   float *acc_f, *force_f, *extf_f, *vol_f;
+  float dt_f, hdt2_f, half_dt_f;
 };
+
+#ifdef __CUDACC__
+// Warp-wide min / max of 64-bit keys with two 32-bit hardware reductions each (all 32 lanes).
+__device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long k) {
+  const uint32_t hi = (uint32_t)(k >> 32), lo = (uint32_t)k;
+  const uint32_t h = __reduce_min_sync(0xffffffffu, hi);
+  const uint32_t l = __reduce_min_sync(0xffffffffu, hi == h ? lo : 0xffffffffu);
+  return ((unsigned long long)h << 32) | l;
+}
+__device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long k) {
+  const uint32_t hi = (uint32_t)(k >> 32), lo = (uint32_t)k;
+  const uint32_t h = __reduce_max_sync(0xffffffffu, hi);
+  const uint32_t l = __reduce_max_sync(0xffffffffu, hi == h ? lo : 0u);
+  return ((unsigned long long)h << 32) | l;
+}
+#endif
 
 __host__ __device__ inline unsigned long long dbl_to_ordered(double x) {
   unsigned long long b;

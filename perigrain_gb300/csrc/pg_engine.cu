@@ -148,25 +148,31 @@ static void pack_f(const double* x, uint32_t N, uint32_t D, std::vector<float>* 
 static int mixed_setup(pg_handle* h, const pg_setup_desc* s) {
   Dev& P = h->P;
   const uint32_t N = P.N, D = h->dim, SF = (D == 2) ? 2 : 4;
-  CU(h->dalloc(&P.disp_hl, (size_t)N * 2 * SF));
-  CU(h->dalloc(&P.xpos_hl, (size_t)N * 2 * SF));
+  CU(h->dalloc(&P.bref, (size_t)N * 4 * SF));
   CU(h->dalloc(&P.cur_hl, (size_t)N * 2 * SF));
   CU(h->dalloc(&P.acc_f, (size_t)N * SF));
   CU(h->dalloc(&P.force_f, (size_t)N * SF));
   CU(h->dalloc(&P.extf_f, (size_t)N * SF));
   CU(h->dalloc(&P.vol_f, N));
+  P.dt_f = (float)P.dt;
+  P.hdt2_f = (float)P.hdt2;
+  P.half_dt_f = (float)P.half_dt;
   std::vector<double> org((size_t)N * 3, 0.0);
   for (uint32_t g = 0; g < P.G; ++g) {
     const InstDev& in = h->inst_host[s->grain_instance[g]];
     for (uint32_t i = s->grain_node_offset[g]; i < s->grain_node_offset[g + 1]; ++i)
       for (uint32_t c = 0; c < 3; ++c) org[(size_t)i * 3 + c] = in.xorigin[c];
   }
-  std::vector<float> tmp;
-  pack_hl(s->pos, N, D, &org, &tmp);
-  CU(cudaMemcpy(P.xpos_hl, tmp.data(), tmp.size() * 4, cudaMemcpyHostToDevice));
-  CU(cudaMemset(P.cur_hl, 0, tmp.size() * 4));
+  std::vector<float> tmp, xr, ref((size_t)N * 4 * SF, 0.f);
   pack_hl(s->disp, N, D, nullptr, &tmp);
-  CU(cudaMemcpy(P.disp_hl, tmp.data(), tmp.size() * 4, cudaMemcpyHostToDevice));
+  pack_hl(s->pos, N, D, &org, &xr);
+  for (uint32_t i = 0; i < N; ++i)
+    for (uint32_t k = 0; k < 2 * SF; ++k) {
+      ref[(size_t)i * 4 * SF + k] = tmp[(size_t)i * 2 * SF + k];
+      ref[(size_t)i * 4 * SF + 2 * SF + k] = xr[(size_t)i * 2 * SF + k];
+    }
+  CU(cudaMemcpy(P.bref, ref.data(), ref.size() * 4, cudaMemcpyHostToDevice));
+  CU(cudaMemset(P.cur_hl, 0, (size_t)N * 2 * SF * 4));
   pack_f(s->acc, N, D, &tmp);
   CU(cudaMemcpy(P.acc_f, tmp.data(), tmp.size() * 4, cudaMemcpyHostToDevice));
   pack_f(s->extforce, N, D, &tmp);
@@ -800,8 +806,13 @@ int pg_set_field(pg_handle* h, int field, const double* in) {
   if (h->precision == PG_MIXED && (field == PG_FIELD_DISP || field == PG_FIELD_ACC)) {
     std::vector<float> tf;
     if (field == PG_FIELD_DISP) {
+      const uint32_t SF = (D == 2) ? 2 : 4;
+      std::vector<float> ref((size_t)N * 4 * SF);
+      CU(cudaMemcpy(ref.data(), h->P.bref, ref.size() * 4, cudaMemcpyDeviceToHost));
       pack_hl(in, N, D, nullptr, &tf);
-      CU(cudaMemcpy(h->P.disp_hl, tf.data(), tf.size() * 4, cudaMemcpyHostToDevice));
+      for (uint32_t i = 0; i < N; ++i)
+        for (uint32_t k = 0; k < 2 * SF; ++k) ref[(size_t)i * 4 * SF + k] = tf[(size_t)i * 2 * SF + k];
+      CU(cudaMemcpy(h->P.bref, ref.data(), ref.size() * 4, cudaMemcpyHostToDevice));
     } else {
       pack_f(in, N, D, &tf);
       CU(cudaMemcpy(h->P.acc_f, tf.data(), tf.size() * 4, cudaMemcpyHostToDevice));

@@ -94,29 +94,19 @@ __global__ void __launch_bounds__(256) k_predict(const Dev P) {
   uint32_t same = __ballot_sync(full, !act || g == g0);
   if (same == full) {
     for (int c = 0; c < D; ++c) {
-      for (int off = 16; off > 0; off >>= 1) {
-        unsigned long long o1 = __shfl_down_sync(full, kmin[c], off);
-        unsigned long long o2 = __shfl_down_sync(full, kmax[c], off);
-        kmin[c] = o1 < kmin[c] ? o1 : kmin[c];
-        kmax[c] = o2 > kmax[c] ? o2 : kmax[c];
-      }
+      kmin[c] = warp_min_u64(kmin[c]);
+      kmax[c] = warp_max_u64(kmax[c]);
     }
     if (lane == 0) {
-      const uint32_t i0 = P.grain[g0].inst;
       for (int c = 0; c < D; ++c) {
         atomicMin(&P.bbox[(size_t)g0 * 2 * D + c], kmin[c]);
         atomicMax(&P.bbox[(size_t)g0 * 2 * D + D + c], kmax[c]);
-        atomicMin(&P.ibox[(size_t)i0 * 2 * D + c], kmin[c]);
-        atomicMax(&P.ibox[(size_t)i0 * 2 * D + D + c], kmax[c]);
       }
     }
   } else if (act) {
-    const uint32_t i0 = P.grain[g].inst;
     for (int c = 0; c < D; ++c) {
       atomicMin(&P.bbox[(size_t)g * 2 * D + c], kmin[c]);
       atomicMax(&P.bbox[(size_t)g * 2 * D + D + c], kmax[c]);
-      atomicMin(&P.ibox[(size_t)i0 * 2 * D + c], kmin[c]);
-      atomicMax(&P.ibox[(size_t)i0 * 2 * D + D + c], kmax[c]);
     }
   }
 }

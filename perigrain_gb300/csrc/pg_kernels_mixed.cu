@@ -33,28 +33,27 @@ __device__ __forceinline__ float trunc_f32(double x, double* as_double) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(x);
   const unsigned int hw = (unsigned int)(b >> 32);
   const int e = (int)((hw >> 20) & 0x7ffu);
-  if (e < 1023 - 126) {
+  const unsigned int sgn = hw & 0x80000000u;
+  if (e < 1023 - 126) {  // below the FP32 normal range: 0
     *as_double = 0.0;
-    return 0.f;
+    return __uint_as_float(sgn);
   }
-  if (e > 1023 + 127) {
-    const float f = (float)x;
-    *as_double = (double)f;
-    return f;
+  if (e > 1023 + 127) {  // beyond FP32 (inf/NaN included): inf or NaN, and lo = x - x
+    *as_double = x;
+    const bool nan = (e == 0x7ff) && ((b & 0xfffffffffffffull) != 0);
+    return __uint_as_float(sgn | 0x7f800000u | (nan ? 0x400000u : 0u));
   }
   *as_double = __longlong_as_double((long long)(b & ~((1ull << 29) - 1)));
-  return __uint_as_float((hw & 0x80000000u) | ((unsigned int)(e - 896) << 23) |
-                         (unsigned int)((b >> 29) & 0x7fffffu));
+  return __uint_as_float(sgn | ((unsigned int)(e - 896) << 23) | (unsigned int)((b >> 29) & 0x7fffffu));
 }
-// Exact widening of a float; zero and subnormal floats become a signed zero.
+// Exact widening of a float; subnormal floats become a signed zero.
 __device__ __forceinline__ double widen(float f) {
   const unsigned int b = __float_as_uint(f);
   const unsigned int e = (b >> 23) & 0xffu;
   const unsigned long long sgn = (unsigned long long)(b & 0x80000000u) << 32;
   if (e == 0) return __longlong_as_double((long long)sgn);
-  if (e == 0xff) return (double)f;
-  return __longlong_as_double((long long)(sgn | ((unsigned long long)(e + 896) << 52) |
-                                          ((unsigned long long)(b & 0x7fffffu) << 29)));
+  const unsigned long long ee = (e == 0xff) ? 0x7ffull : (unsigned long long)(e + 896);
+  return __longlong_as_double((long long)(sgn | (ee << 52) | ((unsigned long long)(b & 0x7fffffu) << 29)));
 }
 // hi/lo pair: x = hi + lo + O(2^-47 |x|)
 __device__ __forceinline__ void split_hl(double x, float* hi, float* lo) {
@@ -82,6 +81,39 @@ __device__ __forceinline__ void ld_hl(const float* a, uint32_t i, float (&h)[D],
     l[2] = t1.z;
   }
 }
+// bref record of node i: [disp hi, disp lo, xpos hi, xpos lo], each SF floats
+template <int D>
+__device__ __forceinline__ void ld_ref(const float* bref, uint32_t i, float (&dh)[D], float (&dl)[D],
+                                       float (&xh)[D], float (&xl)[D]) {
+  if constexpr (D == 2) {
+    const float4* p = reinterpret_cast<const float4*>(bref) + 2ull * i;
+    const float4 a = p[0], b = p[1];
+    dh[0] = a.x;
+    dh[1] = a.y;
+    dl[0] = a.z;
+    dl[1] = a.w;
+    xh[0] = b.x;
+    xh[1] = b.y;
+    xl[0] = b.z;
+    xl[1] = b.w;
+  } else {
+    const float4* p = reinterpret_cast<const float4*>(bref) + 4ull * i;
+    const float4 a = p[0], b = p[1], c = p[2], e = p[3];
+    dh[0] = a.x;
+    dh[1] = a.y;
+    dh[2] = a.z;
+    dl[0] = b.x;
+    dl[1] = b.y;
+    dl[2] = b.z;
+    xh[0] = c.x;
+    xh[1] = c.y;
+    xh[2] = c.z;
+    xl[0] = e.x;
+    xl[1] = e.y;
+    xl[2] = e.z;
+  }
+}
+
 template <int D>
 __device__ __forceinline__ void st_hl(float* a, uint32_t i, const double (&x)[D]) {
   float h[D], l[D];
@@ -150,16 +182,15 @@ __global__ void __launch_bounds__(256) k_predict_mx(const Dev P) {
       float a[D];
       ldv<D>(P.vel_in, d, v);
       ldvf<D>(P.acc_f, d, a);
-      const float dtf = (float)P.dt, hdt2f = (float)P.hdt2;
       for (int c = 0; c < D; ++c) {
         const float vf = trunc_f32(v[c], &vd);
-        dp[c] = dp[c] + widen(fmaf(dtf, vf, hdt2f * a[c]));
+        dp[c] = dp[c] + widen(fmaf(P.dt_f, vf, P.hdt2_f * a[c]));
       }
       wrote = true;
     }
     if (wrote) {
       stv<D>(P.disp, d, dp);
-      st_hl<D>(P.disp_hl, d, dp);
+      st_hl<D>(P.bref, 2 * d, dp);  // first half of record d
     }
     ldv<D>(P.pos, d, ps);
     for (int c = 0; c < D; ++c) cu[c] = ps[c] + dp[c];
@@ -210,29 +241,19 @@ __global__ void __launch_bounds__(256) k_predict_mx(const Dev P) {
   uint32_t same = __ballot_sync(full, !act || g == g0);
   if (same == full) {
     for (int c = 0; c < D; ++c) {
-      for (int off = 16; off > 0; off >>= 1) {
-        unsigned long long o1 = __shfl_down_sync(full, kmin[c], off);
-        unsigned long long o2 = __shfl_down_sync(full, kmax[c], off);
-        kmin[c] = o1 < kmin[c] ? o1 : kmin[c];
-        kmax[c] = o2 > kmax[c] ? o2 : kmax[c];
-      }
+      kmin[c] = warp_min_u64(kmin[c]);
+      kmax[c] = warp_max_u64(kmax[c]);
     }
     if (lane == 0) {
-      const uint32_t i0 = P.grain[g0].inst;
       for (int c = 0; c < D; ++c) {
         atomicMin(&P.bbox[(size_t)g0 * 2 * D + c], kmin[c]);
         atomicMax(&P.bbox[(size_t)g0 * 2 * D + D + c], kmax[c]);
-        atomicMin(&P.ibox[(size_t)i0 * 2 * D + c], kmin[c]);
-        atomicMax(&P.ibox[(size_t)i0 * 2 * D + D + c], kmax[c]);
       }
     }
   } else if (act) {
-    const uint32_t i0 = P.grain[g].inst;
     for (int c = 0; c < D; ++c) {
       atomicMin(&P.bbox[(size_t)g * 2 * D + c], kmin[c]);
       atomicMax(&P.bbox[(size_t)g * 2 * D + D + c], kmax[c]);
-      atomicMin(&P.ibox[(size_t)i0 * 2 * D + c], kmin[c]);
-      atomicMax(&P.ibox[(size_t)i0 * 2 * D + D + c], kmax[c]);
     }
   }
 }
@@ -273,24 +294,22 @@ __global__ void __launch_bounds__(128) k_force_mx(const Dev P) {
   const uint32_t g = act ? P.node_grain[d] : 0;
   const GrainDev gr = P.grain[g];
   const bool mov = act && (gr.flags & GF_MOVABLE);
-  const bool brk = P.enable_fracture && (gr.flags & GF_BREAKABLE) && (gr.flags & GF_BREAK_BONDS);
-  const float cnot = (float)gr.cnot, snot = (float)gr.snot;
 
   float f[D];
   for (int c = 0; c < D; ++c) f[c] = 0.f;
   double vpd[D];
   if (act) ldv<D>(P.vel_in, d, vpd);
 
+  const bool brk = P.enable_fracture && (gr.flags & GF_BREAKABLE) && (gr.flags & GF_BREAK_BONDS);
+  const float cnot = (float)gr.cnot, snot = (float)gr.snot;
   const uint32_t cdeg = P.chunk_deg[chunk];
   const uint32_t slot0 = P.chunk_slot[chunk] + lane;
   const uint32_t w0 = P.chunk_word[chunk];
   {
+    // bond forces and bond breaking (particle2.h:102-232): two bonds per iteration, both
+    // neighbour gathers issued before either is used
     float dh[D], dl[D], xh[D], xl[D];
-    if (mov) {
-      ld_hl<D>(P.disp_hl, d, dh, dl);
-      ld_hl<D>(P.xpos_hl, d, xh, xl);
-    }
-    // two bonds per iteration: both neighbour gathers are issued before either is used
+    if (mov) ld_ref<D>(P.bref, d, dh, dl, xh, xl);
     for (uint32_t k = 0; k < cdeg; k += 2) {
       const bool two = (k + 1) < cdeg;
       const uint32_t wa = P.alive[w0 + k];
@@ -301,10 +320,8 @@ __global__ void __launch_bounds__(128) k_force_mx(const Dev P) {
       const uint32_t ja = ua ? P.bcol[sa] : d;
       const uint32_t jb = ub ? P.bcol[sb] : d;
       float adh[D], adl[D], axh[D], axl[D], bdh[D], bdl[D], bxh[D], bxl[D];
-      ld_hl<D>(P.disp_hl, ja, adh, adl);
-      ld_hl<D>(P.xpos_hl, ja, axh, axl);
-      ld_hl<D>(P.disp_hl, jb, bdh, bdl);
-      ld_hl<D>(P.xpos_hl, jb, bxh, bxl);
+      ld_ref<D>(P.bref, ja, adh, adl, axh, axl);
+      ld_ref<D>(P.bref, jb, bdh, bdl, bxh, bxl);
       const float va = P.vol_f[ja], vb = P.vol_f[jb];
       float stra, strb;
       bond_term<D>(dh, dl, xh, xl, adh, adl, axh, axl, cnot * va, ua, f, &stra);
@@ -325,6 +342,7 @@ __global__ void __launch_bounds__(128) k_force_mx(const Dev P) {
       }
     }
   }
+  __syncwarp();
   __syncwarp();
 
   unsigned long long my_pairs = 0, my_hash = 0, my_close = 0;
@@ -575,7 +593,7 @@ __global__ void __launch_bounds__(128) k_force_mx(const Dev P) {
       float ao[D], a[D];
       double v[D];
       ldvf<D>(P.acc_f, d, ao);
-      const float orho = (float)gr.one_over_rho, hdt = (float)P.half_dt;
+      const float orho = (float)gr.one_over_rho, hdt = P.half_dt_f;
       for (int c = 0; c < D; ++c) {
         a[c] = orho * f[c];
         v[c] = vpd[c] + widen((ao[c] + a[c]) * hdt);  // FP64 accumulation of an FP32 increment
@@ -611,6 +629,7 @@ __global__ void __launch_bounds__(128) k_force_mx(const Dev P) {
 template <int D>
 static void launch_mx(const Dev& P, const LaunchCfg& L, cudaStream_t s, uint64_t* launches, cudaEvent_t e0,
                       cudaEvent_t e1) {
+  const uint32_t nthr = P.n_chunks * 32;
   k_predict_mx<D><<<cdiv(P.N, 256), 256, 0, s>>>(P);
   *launches += 1;
   launch_grid_build(P, s, launches);
@@ -619,7 +638,7 @@ static void launch_mx(const Dev& P, const LaunchCfg& L, cudaStream_t s, uint64_t
     *launches += 1;
   }
   if (e0) cudaEventRecord(e0, s);
-  k_force_mx<D><<<cdiv(P.n_chunks * 32, L.force_block), L.force_block, 0, s>>>(P);
+  k_force_mx<D><<<cdiv(nthr, L.force_block), L.force_block, 0, s>>>(P);
   if (e1) cudaEventRecord(e1, s);
   k_finalize<D><<<1, FINAL_THREADS, WREC_SMEM_CAP * sizeof(unsigned long long), s>>>(P);
   *launches += 2;
