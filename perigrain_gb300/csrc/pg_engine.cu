@@ -148,7 +148,7 @@ static void pack_f(const double* x, uint32_t N, uint32_t D, std::vector<float>* 
 static int mixed_setup(pg_handle* h, const pg_setup_desc* s) {
   Dev& P = h->P;
   const uint32_t N = P.N, D = h->dim, SF = (D == 2) ? 2 : 4;
-  CU(h->dalloc(&P.bref, (size_t)N * 4 * SF));
+  CU(h->dalloc(&P.bref, (size_t)N * 4 * D));
   CU(h->dalloc(&P.cur_hl, (size_t)N * 2 * SF));
   CU(h->dalloc(&P.acc_f, (size_t)N * SF));
   CU(h->dalloc(&P.force_f, (size_t)N * SF));
@@ -163,13 +163,21 @@ static int mixed_setup(pg_handle* h, const pg_setup_desc* s) {
     for (uint32_t i = s->grain_node_offset[g]; i < s->grain_node_offset[g + 1]; ++i)
       for (uint32_t c = 0; c < 3; ++c) org[(size_t)i * 3 + c] = in.xorigin[c];
   }
-  std::vector<float> tmp, xr, ref((size_t)N * 4 * SF, 0.f);
+  std::vector<float> tmp, xr, ref((size_t)N * 4 * D, 0.f);
   pack_hl(s->disp, N, D, nullptr, &tmp);
   pack_hl(s->pos, N, D, &org, &xr);
+  // 2D: per-node record [disp hi, disp lo, xpos hi, xpos lo]; 3D: planes in that order
   for (uint32_t i = 0; i < N; ++i)
-    for (uint32_t k = 0; k < 2 * SF; ++k) {
-      ref[(size_t)i * 4 * SF + k] = tmp[(size_t)i * 2 * SF + k];
-      ref[(size_t)i * 4 * SF + 2 * SF + k] = xr[(size_t)i * 2 * SF + k];
+    for (uint32_t c = 0; c < D; ++c) {
+      const float v[4] = {tmp[(size_t)i * 2 * SF + c], tmp[(size_t)i * 2 * SF + SF + c], xr[(size_t)i * 2 * SF + c],
+                          xr[(size_t)i * 2 * SF + SF + c]};
+      for (uint32_t q = 0; q < 4; ++q) {
+        if (D == 2) {
+          ref[(size_t)i * 8 + q * 2 + c] = v[q];
+        } else {
+          ref[(size_t)(q * D + c) * N + i] = v[q];
+        }
+      }
     }
   CU(cudaMemcpy(P.bref, ref.data(), ref.size() * 4, cudaMemcpyHostToDevice));
   CU(cudaMemset(P.cur_hl, 0, (size_t)N * 2 * SF * 4));
@@ -807,11 +815,20 @@ int pg_set_field(pg_handle* h, int field, const double* in) {
     std::vector<float> tf;
     if (field == PG_FIELD_DISP) {
       const uint32_t SF = (D == 2) ? 2 : 4;
-      std::vector<float> ref((size_t)N * 4 * SF);
-      CU(cudaMemcpy(ref.data(), h->P.bref, ref.size() * 4, cudaMemcpyDeviceToHost));
       pack_hl(in, N, D, nullptr, &tf);
+      std::vector<float> ref((size_t)N * 4 * D);
+      CU(cudaMemcpy(ref.data(), h->P.bref, ref.size() * 4, cudaMemcpyDeviceToHost));
       for (uint32_t i = 0; i < N; ++i)
-        for (uint32_t k = 0; k < 2 * SF; ++k) ref[(size_t)i * 4 * SF + k] = tf[(size_t)i * 2 * SF + k];
+        for (uint32_t c = 0; c < D; ++c) {
+          const float hv = tf[(size_t)i * 2 * SF + c], lv = tf[(size_t)i * 2 * SF + SF + c];
+          if (D == 2) {
+            ref[(size_t)i * 8 + c] = hv;
+            ref[(size_t)i * 8 + 2 + c] = lv;
+          } else {
+            ref[(size_t)c * N + i] = hv;
+            ref[(size_t)(D + c) * N + i] = lv;
+          }
+        }
       CU(cudaMemcpy(h->P.bref, ref.data(), ref.size() * 4, cudaMemcpyHostToDevice));
     } else {
       pack_f(in, N, D, &tf);

@@ -81,13 +81,16 @@ __device__ __forceinline__ void ld_hl(const float* a, uint32_t i, float (&h)[D],
     l[2] = t1.z;
   }
 }
-// bref record of node i: [disp hi, disp lo, xpos hi, xpos lo], each SF floats
+// bref layout. 2D: one 32-byte record per node, [disp hi.xy, disp lo.xy, xpos hi.xy, xpos lo.xy]
+// (a neighbour gather touches one sector). 3D: 4*3 planes of N floats -- disp hi, disp lo, xpos
+// hi, xpos lo (a padded 3D record would span two sectors; planes keep a warp's gather of the k-th
+// neighbours of 32 consecutive nodes on consecutive entries).
 template <int D>
-__device__ __forceinline__ void ld_ref(const float* bref, uint32_t i, float (&dh)[D], float (&dl)[D],
-                                       float (&xh)[D], float (&xl)[D]) {
+__device__ __forceinline__ void ld_ref(const float* __restrict__ bref, uint32_t N, uint32_t i, float (&dh)[D],
+                                       float (&dl)[D], float (&xh)[D], float (&xl)[D]) {
   if constexpr (D == 2) {
     const float4* p = reinterpret_cast<const float4*>(bref) + 2ull * i;
-    const float4 a = p[0], b = p[1];
+    const float4 a = __ldg(p), b = __ldg(p + 1);
     dh[0] = a.x;
     dh[1] = a.y;
     dl[0] = a.z;
@@ -97,20 +100,25 @@ __device__ __forceinline__ void ld_ref(const float* bref, uint32_t i, float (&dh
     xl[0] = b.z;
     xl[1] = b.w;
   } else {
-    const float4* p = reinterpret_cast<const float4*>(bref) + 4ull * i;
-    const float4 a = p[0], b = p[1], c = p[2], e = p[3];
-    dh[0] = a.x;
-    dh[1] = a.y;
-    dh[2] = a.z;
-    dl[0] = b.x;
-    dl[1] = b.y;
-    dl[2] = b.z;
-    xh[0] = c.x;
-    xh[1] = c.y;
-    xh[2] = c.z;
-    xl[0] = e.x;
-    xl[1] = e.y;
-    xl[2] = e.z;
+    for (int c = 0; c < D; ++c) {
+      dh[c] = __ldg(bref + (size_t)c * N + i);
+      dl[c] = __ldg(bref + (size_t)(D + c) * N + i);
+      xh[c] = __ldg(bref + (size_t)(2 * D + c) * N + i);
+      xl[c] = __ldg(bref + (size_t)(3 * D + c) * N + i);
+    }
+  }
+}
+template <int D>
+__device__ __forceinline__ void st_ref_disp(float* bref, uint32_t N, uint32_t i, const double (&x)[D]) {
+  float h[D], l[D];
+  for (int c = 0; c < D; ++c) split_hl(x[c], &h[c], &l[c]);
+  if constexpr (D == 2) {
+    reinterpret_cast<float4*>(bref)[2ull * i] = make_float4(h[0], h[1], l[0], l[1]);
+  } else {
+    for (int c = 0; c < D; ++c) {
+      bref[(size_t)c * N + i] = h[c];
+      bref[(size_t)(D + c) * N + i] = l[c];
+    }
   }
 }
 
@@ -190,7 +198,7 @@ __global__ void __launch_bounds__(256) k_predict_mx(const Dev P) {
     }
     if (wrote) {
       stv<D>(P.disp, d, dp);
-      st_hl<D>(P.bref, 2 * d, dp);  // first half of record d
+      st_ref_disp<D>(P.bref, P.N, d, dp);
     }
     ldv<D>(P.pos, d, ps);
     for (int c = 0; c < D; ++c) cu[c] = ps[c] + dp[c];
@@ -309,7 +317,7 @@ __global__ void __launch_bounds__(128) k_force_mx(const Dev P) {
     // bond forces and bond breaking (particle2.h:102-232): two bonds per iteration, both
     // neighbour gathers issued before either is used
     float dh[D], dl[D], xh[D], xl[D];
-    if (mov) ld_ref<D>(P.bref, d, dh, dl, xh, xl);
+    if (mov) ld_ref<D>(P.bref, P.N, d, dh, dl, xh, xl);
     for (uint32_t k = 0; k < cdeg; k += 2) {
       const bool two = (k + 1) < cdeg;
       const uint32_t wa = P.alive[w0 + k];
@@ -320,8 +328,8 @@ __global__ void __launch_bounds__(128) k_force_mx(const Dev P) {
       const uint32_t ja = ua ? P.bcol[sa] : d;
       const uint32_t jb = ub ? P.bcol[sb] : d;
       float adh[D], adl[D], axh[D], axl[D], bdh[D], bdl[D], bxh[D], bxl[D];
-      ld_ref<D>(P.bref, ja, adh, adl, axh, axl);
-      ld_ref<D>(P.bref, jb, bdh, bdl, bxh, bxl);
+      ld_ref<D>(P.bref, P.N, ja, adh, adl, axh, axl);
+      ld_ref<D>(P.bref, P.N, jb, bdh, bdl, bxh, bxl);
       const float va = P.vol_f[ja], vb = P.vol_f[jb];
       float stra, strb;
       bond_term<D>(dh, dl, xh, xl, adh, adl, axh, axl, cnot * va, ua, f, &stra);
