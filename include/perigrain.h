@@ -188,6 +188,57 @@ int pg_get_launch_count(pg_handle* h, uint64_t* launches);
 int pg_set_timing(pg_handle* h, int32_t enable);
 int pg_get_kernel_times(pg_handle* h, double* force_ms, double* total_ms, uint64_t* force_launches);
 
+/* ---- gradients ------------------------------------------------------------------------------ */
+/* The reference has no gradient path; these entry points differentiate its time step
+ * (timeloop.h:608-879, the run_timeloop body) with respect to per-grain parameters.
+ *
+ * Parameters per grain g, in this order (PG_NPARAM): cnot (bond stiffness, particle2.h:140; it
+ * also sets the self-contact stiffness cnot/R_c', contact.h:709-730), normal contact stiffness,
+ * damping ratio, friction coefficient. Two grains in contact use the mean of their values; with
+ * equal values this is the reference's global Contact parameters (contact.h:43-112), and grain g
+ * meets a wall with its own values. The gradient is that of the run with its masks frozen: bond
+ * breaks, contact pairs, friction branches (sliding or sticking) and wall contacts stay as the
+ * forward pass decided them. Torque (enable_torque) is not differentiated: PG_EINVAL. Every
+ * movable grain must be stoppable (the adjoint gathers each contact pair at both nodes).
+ *
+ * Usage: pg_grad_begin marks the current state as the origin; pg_grad_forward runs n_steps from
+ * the origin keeping a checkpoint of the state every checkpoint_every steps; the caller reads the
+ * objectives (pg_get_field, pg_get_reaction); pg_grad_backward recomputes each segment from its
+ * checkpoint (recording the masks) and runs the reverse steps, leaving the handle at the final
+ * state again. Memory: one checkpoint per segment plus one segment of tape. */
+#define PG_NPARAM 4
+/* Per-grain parameters; any pointer may be NULL (left unchanged). Setting kn, zeta or mu makes
+ * the force kernels use the per-grain contact parameters. snot (critical stretch) has no
+ * gradient (bond breaks are frozen) but is settable so cnot and snot can follow one modulus. */
+int pg_set_grain_params(pg_handle* h, const double* cnot, const double* snot, const double* kn,
+                        const double* zeta, const double* mu);
+int pg_get_grain_params(pg_handle* h, double* cnot, double* snot, double* kn, double* zeta, double* mu);
+/* Mark the current state as the origin of differentiable runs. */
+int pg_grad_begin(pg_handle* h);
+/* Restore the origin state. */
+int pg_grad_reset(pg_handle* h);
+/* Masks of a run recorded once and replayed by frozen forwards (finite-difference checks and
+ * FP64 reference gradients). */
+typedef struct pg_masks pg_masks;
+/* From the origin, run n_steps with the handle's own precision, recording the masks of every
+ * step (contact entries, wall bits, bond breaks). Leaves the handle at the end of the run. */
+int pg_masks_record(pg_handle* h, uint32_t n_steps, pg_masks** out);
+void pg_masks_free(pg_masks* m);
+/* From the origin, run n_steps keeping a checkpoint every checkpoint_every steps. frozen = NULL:
+ * the handle's own step (FP64 or mixed precision); otherwise an FP64 step that replays the
+ * masks of `frozen` (recorded from this origin, n_steps <= its length) instead of deciding
+ * them. */
+int pg_grad_forward(pg_handle* h, uint32_t n_steps, uint32_t checkpoint_every, const pg_masks* frozen);
+/* Cotangents of the last forward's final state -- disp_bar, vel_bar [n_nodes*dim] (NULL = 0) and
+ * of its last step's wall reactions reaction_bar [n_instances*2*dim*dim] (NULL = 0) -- to
+ * grad[n_grains*PG_NPARAM], the gradient with respect to the per-grain parameters. */
+int pg_grad_backward(pg_handle* h, const double* disp_bar, const double* vel_bar, const double* reaction_bar,
+                     double* grad);
+/* Device time of the last pg_grad_forward / pg_grad_backward (CUDA events) and their kernel
+ * launch counts. */
+int pg_grad_times(pg_handle* h, double* forward_ms, double* backward_ms, uint64_t* forward_launches,
+                  uint64_t* backward_launches);
+
 /* ---- setup helpers -------------------------------------------------------------------------- */
 /* Bond list of one grain on the GPU: every node pair (i, j), i < j, with
  * sqrt(sum_c (p_j[c] - p_i[c])^2) <= delta, rows in lexicographic order -- the Connectivity the

@@ -107,6 +107,16 @@ PROTOTYPES = [
     ("pg_build_bonds_noalloc", C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_double, C.c_void_p, C.c_uint64,
                                          u64p, C.c_void_p]),
     ("pg_noalloc_last_error", C.c_char_p, []),
+    # gradients
+    ("pg_set_grain_params", C.c_int, [C.c_void_p, f64p, f64p, f64p, f64p, f64p]),
+    ("pg_get_grain_params", C.c_int, [C.c_void_p, f64p, f64p, f64p, f64p, f64p]),
+    ("pg_grad_begin", C.c_int, [C.c_void_p]),
+    ("pg_grad_reset", C.c_int, [C.c_void_p]),
+    ("pg_masks_record", C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(C.c_void_p)]),
+    ("pg_masks_free", None, [C.c_void_p]),
+    ("pg_grad_forward", C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p]),
+    ("pg_grad_backward", C.c_int, [C.c_void_p, f64p, f64p, f64p, f64p]),
+    ("pg_grad_times", C.c_int, [C.c_void_p, f64p, f64p, u64p, u64p]),
     # perigrain_io.h
     ("pg_conf_default", None, [C.POINTER(Conf)]),
     ("pg_conf_read_file", C.c_int, [C.POINTER(Conf), C.c_char_p]),

@@ -23,7 +23,8 @@ LIB = os.path.join(HERE, "libperigrain.so")
 BIN = os.path.join(HERE, "bin")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["pg_kernels.cu", "pg_kernels_mixed.cu", "pg_engine.cu", "pg_bonds.cu", "pg_noalloc.cu"]
+CU_SOURCES = ["pg_kernels.cu", "pg_kernels_mixed.cu", "pg_engine.cu", "pg_bonds.cu", "pg_noalloc.cu",
+              "pg_adjoint.cu", "pg_adjoint_rev.cu", "pg_grad.cu"]
 CXX_SOURCES = ["h5lite.cpp", "pg_io.cpp"]
 
 
@@ -60,8 +61,9 @@ def build(verbose=False, force=False):
         s = os.path.join(CSRC, src)
         o = os.path.join(BUILD, src + ".o")
         objs.append(o)
-        # the mixed-precision kernels use FMA; everything else performs the reference's exact ops
-        fmad = "--fmad=true" if src == "pg_kernels_mixed.cu" else "--fmad=false"
+        # the mixed-precision kernels and the reverse step use FMA; everything else performs the
+        # reference's exact ops
+        fmad = "--fmad=true" if src in ("pg_kernels_mixed.cu", "pg_adjoint_rev.cu") else "--fmad=false"
         if force or _stale(o, [s] + headers):
             jobs.append([nvcc] + ARCH + ["-O3", fmad, "-lineinfo", "-std=c++17",
                                          "-Xcompiler", "-fPIC,-ffp-contract=off", "-Xptxas", "-v",

@@ -57,6 +57,49 @@ __device__ __forceinline__ void ldf(const float* a, uint32_t i, float (&v)[D]) {
 
 __device__ __forceinline__ void set_status(int32_t* st, int32_t code) { atomicCAS(st, 0, code); }
 
+// Mask recording: append this node's contact entries to rec_ent (one atomic per warp; the whole
+// warp must call this) and store its offset, count and wall bits. On overflow of rec_cap the
+// node's list is stored empty and PG_ECAPACITY raised, so the host can grow the buffer and redo.
+__device__ __forceinline__ void record_masks(const Dev& P, uint32_t d, bool act, uint32_t lane,
+                                             const uint32_t* rent, uint32_t nrec, uint32_t wbits) {
+  const uint32_t full = 0xffffffffu;
+  uint32_t incl = nrec;
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(full, incl, o);
+    if (lane >= (uint32_t)o) incl += y;
+  }
+  const uint32_t tot = __shfl_sync(full, incl, 31);
+  uint32_t base = 0;
+  if (lane == 31 && tot) base = atomicAdd(P.rec_n, tot);
+  base = __shfl_sync(full, base, 31);
+  if (!act) return;
+  const uint32_t o = base + incl - nrec;
+  if ((uint64_t)o + nrec <= (uint64_t)P.rec_cap) {
+    for (uint32_t i = 0; i < nrec; ++i) P.rec_ent[o + i] = rent[i];
+    P.rec_off[d] = o;
+    P.rec_cnt[d] = (uint8_t)nrec;
+  } else {
+    set_status(P.status, PG_ECAPACITY);
+    P.rec_off[d] = 0;
+    P.rec_cnt[d] = 0;
+  }
+  P.rec_wall[d] = wbits;
+}
+
+// Tape of the step (REC with rec_x): the CurrPos and velocity node d's forces saw, and (first
+// threads) the wall positions and the step number.
+template <int D>
+__device__ __forceinline__ void record_tape(const Dev& P, uint32_t d, bool act, uint32_t t, const double (&x)[D],
+                                            const double (&v)[D]) {
+  if (act) {
+    stv<D>(P.rec_x, d, x);
+    stv<D>(P.rec_v, d, v);
+  }
+  constexpr uint32_t NS = 2 * D;
+  if (d < P.I * NS) P.rec_w[d] = P.inst[d / NS].wall[d % NS];
+  if (d == 0) *P.rec_t = t;
+}
+
 // ---------------------------------------------------------------------------------------------
 // Exclusive scan of cell_count -> cell_start (reduce-then-scan, last block scans tile sums).
 // ---------------------------------------------------------------------------------------------

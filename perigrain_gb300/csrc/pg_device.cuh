@@ -26,6 +26,10 @@ constexpr uint32_t NONE = 0xffffffffu;
 constexpr int MAX_CAND = 64;        // hard cap of contact candidates held per node
 constexpr int FINAL_THREADS = 1024; // threads of the per-step finalize kernel
 constexpr int WREC_SMEM_CAP = 16384;// wall-reaction records sorted in shared memory per step
+constexpr uint32_t ENT_NODE = 0x3fffffffu;  // partner bits of a recorded contact entry
+// friction branch of a recorded contact entry; in 2D a sliding contact also records the sign of
+// its tangential direction along perp(u) = (-u_y, u_x) (FR_SLIDE_NEG when negative)
+constexpr uint32_t FR_SLIDE = 1u, FR_STICK = 2u, FR_SLIDE_NEG = 3u;
 
 enum GrainFlag : uint32_t {
   GF_MOVABLE = 1u,
@@ -42,6 +46,11 @@ struct GrainDev {
   double torque_val;
   uint32_t torque_axis;
   uint32_t pad;
+  // per-grain contact parameters (normal stiffness, damping ratio, friction coefficient); used by
+  // the force kernels only when Dev::grain_contact is set, always by the adjoint. A pair of
+  // grains contacts with the arithmetic mean of the two grains' values, which is the reference's
+  // global parameter when all grains carry the same value.
+  double kn, zeta, mu;
 };
 
 struct InstDev {
@@ -153,6 +162,18 @@ struct Dev {
   int32_t enable_torque, gradient_extforce, record_pairs;
   uint32_t extforce_maxstep;
   uint32_t max_cand;
+  int32_t grain_contact;  // contact parameters from GrainDev (pair mean) instead of InstDev
+  // mask recording (force kernels instantiated with REC = true): per node of this step the
+  // offset and count of its active contact entries in rec_ent (entry = partner | friction
+  // branch << 30, FR_*) and the wall bits (4 per wall side in call order: in contact, friction
+  // active, sticking, 2D sliding towards -t). rec_n counts entries appended so far. When rec_x is
+  // set the kernel also writes the tape of the step: CurrPos and velocity its forces saw (stride
+  // S), the wall positions [I][2D] and the step number.
+  uint32_t *rec_off, *rec_ent, *rec_wall, *rec_n;
+  uint8_t* rec_cnt;
+  uint32_t rec_cap;
+  double *rec_x, *rec_v, *rec_w;
+  uint32_t* rec_t;
   // mixed precision (PG_MIXED): FP32 hi/lo pairs (x = hi + lo to ~2^-47 |x|). `bref` interleaves,
   // per node, the pair of the FP64 displacement and the pair of the bond reference position
   // (relative to the instance's fixed origin) -- 4*SF floats, one 32-byte sector in 2D -- so a bond

@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "pg_device.cuh"
+#include "pg_handle.h"
 #include "pg_kernels.h"
 #include "pg_kernels_mixed.h"
 
@@ -19,77 +20,19 @@ using namespace pg;
 
 static thread_local std::string g_err;
 
-static int fail(int code, const std::string& msg) {
+int pg_fail(int code, const std::string& msg) {
   g_err = msg;
   return code;
 }
 
-#define CU(call)                                                                       \
-  do {                                                                                 \
-    cudaError_t _e = (call);                                                           \
-    if (_e != cudaSuccess)                                                             \
-      return fail(_e == cudaErrorMemoryAllocation ? PG_ENOMEM : PG_ECUDA,              \
-                  std::string(#call) + ": " + cudaGetErrorString(_e));                 \
-  } while (0)
+static int fail(int code, const std::string& msg) { return pg_fail(code, msg); }
 
-struct pg_handle {
-  int device = 0;
-  cudaStream_t stream = nullptr;
-  Dev P{};          // device pointers + config; vel_in/vel_out are set per launch
-  LaunchCfg L;
-  uint32_t dim = 2, S = 2;
-  int precision = PG_FP64;
-  uint64_t next_t = 1;
-  int vel_parity = 0;  // 0: current velocity in vel_a
-  double* vel_a = nullptr;
-  double* vel_b = nullptr;
-  bool xpos_separate = false;
-  std::vector<void*> allocs;
-  // host copies needed for mapping
-  std::vector<uint64_t> bond_offset;  // reference CSR
-  std::vector<uint32_t> grain_node_offset;
-  std::vector<uint32_t> node_deg;
-  std::vector<uint32_t> chunk_slot, chunk_word;
-  std::vector<InstDev> inst_host;
-  // graphs: one per velocity parity, each GRAPH_STEPS steps
-  static const int GRAPH_STEPS = 8;
-  cudaGraphExec_t graph[2] = {nullptr, nullptr};
-  uint64_t graph_launches_per = 0;
-  uint64_t last_launches = 0;
-  // timing
-  bool timing = false;
-  std::vector<cudaEvent_t> ev;
-  double force_ms = 0, total_ms = 0;
-  uint64_t force_launches = 0;
-  cudaEvent_t ev_t0 = nullptr, ev_t1 = nullptr;
-
-  ~pg_handle() {
-    if (stream) cudaStreamSynchronize(stream);
-    for (int i = 0; i < 2; ++i)
-      if (graph[i]) cudaGraphExecDestroy(graph[i]);
-    for (auto e : ev) cudaEventDestroy(e);
-    if (ev_t0) cudaEventDestroy(ev_t0);
-    if (ev_t1) cudaEventDestroy(ev_t1);
-    for (void* p : allocs) cudaFree(p);
-    if (xpos_separate) cudaFree(P.xpos);
-    if (stream) cudaStreamDestroy(stream);
-  }
-
-  template <class T>
-  cudaError_t dalloc(T** p, size_t count) {
-    if (count == 0) count = 1;
-    cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
-    if (e == cudaSuccess) allocs.push_back((void*)*p);
-    return e;
-  }
-};
-
-static void set_vel(pg_handle* h, Dev& P, int parity) {
+void set_vel(pg_handle* h, Dev& P, int parity) {
   P.vel_in = parity == 0 ? h->vel_a : h->vel_b;
   P.vel_out = parity == 0 ? h->vel_b : h->vel_a;
 }
 
-static void enqueue_step(pg_handle* h, int parity, uint64_t* launches) {
+void enqueue_step(pg_handle* h, int parity, uint64_t* launches) {
   Dev P = h->P;
   set_vel(h, P, parity);
   if (h->precision == PG_MIXED) {
@@ -99,7 +42,7 @@ static void enqueue_step(pg_handle* h, int parity, uint64_t* launches) {
   }
 }
 
-static int build_graphs(pg_handle* h) {
+int build_graphs(pg_handle* h) {
   for (int par = 0; par < 2; ++par) {
     if (h->graph[par]) {
       cudaGraphExecDestroy(h->graph[par]);
@@ -516,6 +459,10 @@ static int create_impl(const pg_setup_desc* s, const pg_config* cfg_in, pg_handl
     gd.torque_axis = s->torque_axis ? s->torque_axis[g] : 2;
     gd.torque_val = s->torque_val ? s->torque_val[g] : 0.0;
     gd.pad = 0;
+    // per-grain contact parameters start as the instance's (used once pg_set_grain_params sets them)
+    gd.kn = s->normal_stiffness[s->grain_instance[g]];
+    gd.zeta = s->damping_ratio[s->grain_instance[g]];
+    gd.mu = s->friction_coefficient[s->grain_instance[g]];
   }
   CU(h->dalloc(&P.grain, G));
   CU(cudaMemcpy(P.grain, grains.data(), G * sizeof(GrainDev), cudaMemcpyHostToDevice));
@@ -650,7 +597,9 @@ int pg_destroy(pg_handle* h) {
   return PG_OK;
 }
 
-static int check_device_status(pg_handle* h) {
+}  // extern "C"
+
+int check_device_status(pg_handle* h) {
   int32_t st = 0;
   CU(cudaMemcpyAsync(&st, h->P.status, 4, cudaMemcpyDeviceToHost, h->stream));
   CU(cudaStreamSynchronize(h->stream));
@@ -662,6 +611,8 @@ static int check_device_status(pg_handle* h) {
   }
   return PG_OK;
 }
+
+extern "C" {
 
 int pg_step(pg_handle* h, uint32_t nsteps) {
   if (!h) return fail(PG_EINVAL, "null handle");

@@ -111,7 +111,7 @@ __global__ void __launch_bounds__(256) k_predict(const Dev P) {
   }
 }
 
-template <int D>
+template <int D, bool REC, bool GC>
 __global__ void __launch_bounds__(128) k_force(const Dev P) {
   const uint32_t d = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t lane = threadIdx.x & 31;
@@ -169,6 +169,8 @@ __global__ void __launch_bounds__(128) k_force(const Dev P) {
   __syncwarp();
 
   unsigned long long my_pairs = 0, my_hash = 0, my_close = 0;
+  uint32_t rent[REC ? MAX_CAND : 1];  // recorded contact entries of this node (REC only)
+  uint32_t nrec = 0, wbits = 0;
   const InstDev& in = P.inst[gr.inst];
   const bool p_bdry = !P.nl_bdry_only || (act && P.bdry_rank[d] != NONE);
   const bool selfc = mov && P.enable_fracture && (gr.flags & GF_BREAKABLE) && P.self_contact;
@@ -232,6 +234,13 @@ __global__ void __launch_bounds__(128) k_force(const Dev P) {
       for (int c = 1; c < D; ++c) n2 = n2 + dir[c] * dir[c];
       const double dn = sqrt(n2);
       double Rc = in.contact_rad, Kn = in.normal_stiffness;
+      double zeta = in.damping_ratio, mu = in.friction_coefficient;
+      if constexpr (GC) {
+        const GrainDev& gq = P.grain[(uint32_t)(keys[ci] >> 32) & 0x7fffffffu];
+        Kn = (gr.kn + gq.kn) * 0.5;
+        zeta = (gr.zeta + gq.zeta) * 0.5;
+        mu = (gr.mu + gq.mu) * 0.5;
+      }
       if (same) {
         bool bonded = false;
         for (uint32_t k = 0; k < mydeg && !bonded; ++k) {
@@ -270,6 +279,7 @@ __global__ void __launch_bounds__(128) k_force(const Dev P) {
       for (int c = 1; c < D; ++c) cf2 = cf2 + fc[c] * fc[c];
       const double cfn = sqrt(cf2);
       for (int c = 0; c < D; ++c) f[c] = f[c] + fc[c];
+      uint32_t fr = 0;
       if (P.allow_damping || P.allow_friction) {
         double vq[D], rv[D];
         ldv<D>(P.vel_in, q, vq);
@@ -277,7 +287,7 @@ __global__ void __launch_bounds__(128) k_force(const Dev P) {
         double rvp = rv[0] * u[0];
         for (int c = 1; c < D; ++c) rvp = rvp + rv[c] * u[c];
         if (P.allow_damping) {
-          const double dc = ((2.0 * in.damping_ratio) * sqrt(Kn * gr.rho)) * sqrt(nvol);
+          const double dc = ((2.0 * zeta) * sqrt(Kn * gr.rho)) * sqrt(nvol);
           for (int c = 0; c < D; ++c) f[c] = f[c] + ((-dc) * (rvp * u[c]));
         }
         if (P.allow_friction) {
@@ -287,13 +297,17 @@ __global__ void __launch_bounds__(128) k_force(const Dev P) {
           for (int c = 1; c < D; ++c) t2 = t2 + tg[c] * tg[c];
           const double tn = sqrt(t2);
           if (tn > 0) {
-            const double mu = in.friction_coefficient;
             double sfr = (-mu) * cfn;
-            if (tn < (((mu * cfn) * P.dt) / gr.rho)) sfr = ((-tn) / gr.rho) / P.dt;
+            fr = (D == 2 && (tg[1] * u[0] - tg[0] * u[1]) < 0) ? FR_SLIDE_NEG : FR_SLIDE;
+            if (tn < (((mu * cfn) * P.dt) / gr.rho)) {
+              sfr = ((-tn) / gr.rho) / P.dt;
+              fr = FR_STICK;
+            }
             for (int c = 0; c < D; ++c) f[c] = f[c] + sfr * (tg[c] / tn);
           }
         }
       }
+      if constexpr (REC) rent[nrec++] = q | (fr << 30);
     }
   }
 
@@ -303,6 +317,9 @@ __global__ void __launch_bounds__(128) k_force(const Dev P) {
     grain_box<D>(P, g, bmn, bmx);
     if (!within_interior<D>(bmn, bmx, in.wall, in.contact_rad)) {
       const double vol_i = P.vol[d];
+      const double Knw = GC ? gr.kn : in.normal_stiffness;
+      const double zetaw = GC ? gr.zeta : in.damping_ratio;
+      const double muw = GC ? gr.mu : in.friction_coefficient;
       constexpr int NS = 2 * D;
       // (side, dir) in the reference's call order
       const int order2[4][2] = {{3, 1}, {0, 0}, {1, 0}, {2, 1}};
@@ -313,6 +330,7 @@ __global__ void __launch_bounds__(128) k_force(const Dev P) {
         const double dist = xpc[dir] - in.wall[side];
         const double R = in.contact_rad;
         if (!(fabs(dist) <= R)) continue;
+        wbits |= 1u << (4 * k);
         const double dd = fabs(dist);
         // segment_mass<dim>(R, d) (contact.h:16-41)
         double Area, I;
@@ -326,7 +344,7 @@ __global__ void __launch_bounds__(128) k_force(const Dev P) {
         const double centroid = I / Area;
         const double crc = R - centroid;
         const double pcrc = crc > 0 ? crc : 0;
-        const double F = (in.normal_stiffness * pcrc) * Area;
+        const double F = (Knw * pcrc) * Area;
         const double c_sign = dist > 0 ? 1 : -1;
         f[dir] = f[dir] + (c_sign * F);
         WallRec rec;
@@ -343,13 +361,17 @@ __global__ void __launch_bounds__(128) k_force(const Dev P) {
         for (int c = 0; c < D; ++c) rv[c] = vp[c];
         rv[dir] = rv[dir] - in.wall_speed[side];
         if (P.allow_friction) {
-          const double mu = in.friction_coefficient;
+          const double mu = muw;
           if constexpr (D == 2) {
             const int tg = (dir + 1) % 2;
             if (fabs(rv[tg]) > 0) {
               const double vts = rv[tg] > 0 ? 1 : -1;
               double ff = ((-mu) * fabs(F)) * vts;
-              if (fabs(rv[tg]) < (((mu * fabs(F)) * P.dt) / gr.rho)) ff = ((-rv[tg]) * gr.rho) / P.dt;
+              wbits |= (rv[tg] > 0 ? 2u : 10u) << (4 * k);
+              if (fabs(rv[tg]) < (((mu * fabs(F)) * P.dt) / gr.rho)) {
+                ff = ((-rv[tg]) * gr.rho) / P.dt;
+                wbits |= 4u << (4 * k);
+              }
               f[tg] = f[tg] + ff;
               rec.a_t1 = vol_i * ff;
               rec.has_fric = 1;
@@ -362,9 +384,11 @@ __global__ void __launch_bounds__(128) k_force(const Dev P) {
               const double u1 = v1 / vn, u2 = v2 / vn;
               double ff1 = ((-mu) * fabs(F)) * u1;
               double ff2 = ((-mu) * fabs(F)) * u2;
+              wbits |= 2u << (4 * k);
               if (vn < (((mu * fabs(F)) * P.dt) / gr.rho)) {
                 ff1 = (((-vn) / gr.rho) / P.dt) * u1;
                 ff2 = (((-vn) / gr.rho) / P.dt) * u2;
+                wbits |= 4u << (4 * k);
               }
               f[t1] = f[t1] + ff1;
               f[t2] = f[t2] + ff2;
@@ -375,7 +399,7 @@ __global__ void __launch_bounds__(128) k_force(const Dev P) {
           }
         }
         if (P.allow_damping) {
-          const double dc = ((2.0 * in.damping_ratio) * sqrt(in.normal_stiffness * gr.rho)) * sqrt(fabs(Area));
+          const double dc = ((2.0 * zetaw) * sqrt(Knw * gr.rho)) * sqrt(fabs(Area));
           const double df = (-dc) * rv[dir];
           f[dir] = f[dir] + df;
           rec.a_damp = vol_i * df;
@@ -449,6 +473,11 @@ __global__ void __launch_bounds__(128) k_force(const Dev P) {
     stv<D>(P.force, d, f);  // zero for grains that are not movable
   }
 
+  if constexpr (REC) {
+    record_masks(P, d, act, lane, rent, nrec, wbits);
+    if (P.rec_x) record_tape<D>(P, d, act, t, xpc, vp);
+  }
+
   // ---- diagnostics: warp-aggregated counters ----
   if (P.record_pairs) {
     for (int off = 16; off > 0; off >>= 1) {
@@ -468,7 +497,7 @@ __global__ void __launch_bounds__(128) k_force(const Dev P) {
 // ---------------------------------------------------------------------------------------------
 template <int D>
 static void launch_step_t(const Dev& P, const LaunchCfg& L, cudaStream_t s, uint64_t* launches,
-                          cudaEvent_t e0 = nullptr, cudaEvent_t e1 = nullptr) {
+                          cudaEvent_t e0 = nullptr, cudaEvent_t e1 = nullptr, bool rec = false) {
   const uint32_t nthr_nodes = P.n_chunks * 32;
   k_predict<D><<<cdiv(P.N, 256), 256, 0, s>>>(P);
   *launches += 1;
@@ -478,7 +507,14 @@ static void launch_step_t(const Dev& P, const LaunchCfg& L, cudaStream_t s, uint
     *launches += 1;
   }
   if (e0) cudaEventRecord(e0, s);
-  k_force<D><<<cdiv(nthr_nodes, L.force_block), L.force_block, 0, s>>>(P);
+  const dim3 grid(cdiv(nthr_nodes, L.force_block)), block(L.force_block);
+  if (P.grain_contact) {
+    if (rec) k_force<D, true, true><<<grid, block, 0, s>>>(P);
+    else k_force<D, false, true><<<grid, block, 0, s>>>(P);
+  } else {
+    if (rec) k_force<D, true, false><<<grid, block, 0, s>>>(P);
+    else k_force<D, false, false><<<grid, block, 0, s>>>(P);
+  }
   if (e1) cudaEventRecord(e1, s);
   k_finalize<D><<<1, FINAL_THREADS, WREC_SMEM_CAP * sizeof(unsigned long long), s>>>(P);
   *launches += 2;
@@ -492,11 +528,11 @@ cudaError_t kernels_init() {
                               WREC_SMEM_CAP * (int)sizeof(unsigned long long));
 }
 
-void launch_step(const Dev& P, const LaunchCfg& L, cudaStream_t s, uint64_t* launches) {
+void launch_step(const Dev& P, const LaunchCfg& L, cudaStream_t s, uint64_t* launches, bool rec) {
   if (P.dim == 2) {
-    launch_step_t<2>(P, L, s, launches);
+    launch_step_t<2>(P, L, s, launches, nullptr, nullptr, rec);
   } else {
-    launch_step_t<3>(P, L, s, launches);
+    launch_step_t<3>(P, L, s, launches, nullptr, nullptr, rec);
   }
 }
 
@@ -510,7 +546,7 @@ void launch_step_timed(const Dev& P, const LaunchCfg& L, cudaStream_t s, uint64_
 }
 
 const void* force_kernel_ptr(uint32_t dim) {
-  return dim == 2 ? (const void*)k_force<2> : (const void*)k_force<3>;
+  return dim == 2 ? (const void*)k_force<2, false, false> : (const void*)k_force<3, false, false>;
 }
 
 }  // namespace pg

@@ -14,8 +14,9 @@ struct LaunchCfg {
 };
 
 cudaError_t kernels_init();
-// Enqueue one FP64 time step on stream s. Adds the number of kernel launches to *launches.
-void launch_step(const Dev& P, const LaunchCfg& L, cudaStream_t s, uint64_t* launches);
+// Enqueue one FP64 time step on stream s. Adds the number of kernel launches to *launches. With
+// rec the force kernel also records the step's contact and wall masks (Dev::rec_*).
+void launch_step(const Dev& P, const LaunchCfg& L, cudaStream_t s, uint64_t* launches, bool rec = false);
 // Same as launch_step, with CUDA events e0/e1 recorded around the fused force kernel.
 void launch_step_timed(const Dev& P, const LaunchCfg& L, cudaStream_t s, uint64_t* launches,
                        cudaEvent_t e0, cudaEvent_t e1);

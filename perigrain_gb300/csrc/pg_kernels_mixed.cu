@@ -291,7 +291,7 @@ __device__ __forceinline__ void bond_term(const float (&dh)[D], const float (&dl
 // ---------------------------------------------------------------------------------------------
 // fused force + integrate, FP32 forces
 // ---------------------------------------------------------------------------------------------
-template <int D>
+template <int D, bool REC, bool GC>
 __global__ void __launch_bounds__(128) k_force_mx(const Dev P) {
   const uint32_t d = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t lane = threadIdx.x & 31;
@@ -354,6 +354,8 @@ __global__ void __launch_bounds__(128) k_force_mx(const Dev P) {
   __syncwarp();
 
   unsigned long long my_pairs = 0, my_hash = 0, my_close = 0;
+  uint32_t rent[REC ? MAX_CAND : 1];  // recorded contact entries of this node (REC only)
+  uint32_t nrec = 0, wbits = 0;
   const InstDev& in = P.inst[gr.inst];
   const bool p_bdry = !P.nl_bdry_only || (act && P.bdry_rank[d] != NONE);
   const bool selfc = mov && P.enable_fracture && (gr.flags & GF_BREAKABLE) && P.self_contact;
@@ -407,7 +409,7 @@ __global__ void __launch_bounds__(128) k_force_mx(const Dev P) {
       }
     const uint32_t mydeg = P.node_deg[d];
     const float Rc0 = (float)in.contact_rad, Kn0 = (float)in.normal_stiffness;
-    const float mu = (float)in.friction_coefficient, zeta = (float)in.damping_ratio;
+    const float mu0 = (float)in.friction_coefficient, zeta0 = (float)in.damping_ratio;
     const float rho = (float)gr.rho, dtf = (float)P.dt;
     double xp64[D];
     if (nc) ldv<D>(P.cur, d, xp64);
@@ -424,7 +426,13 @@ __global__ void __launch_bounds__(128) k_force_mx(const Dev P) {
       for (int c = 1; c < D; ++c) n2 = n2 + dir64[c] * dir64[c];
       const double dn64 = sqrt(n2);
       double Rc64 = in.contact_rad;
-      float Kn = Kn0;
+      float Kn = Kn0, zeta = zeta0, mu = mu0;
+      if constexpr (GC) {
+        const GrainDev& gq = P.grain[(uint32_t)(keys[ci] >> 32) & 0x7fffffffu];
+        Kn = (float)((gr.kn + gq.kn) * 0.5);
+        zeta = (float)((gr.zeta + gq.zeta) * 0.5);
+        mu = (float)((gr.mu + gq.mu) * 0.5);
+      }
       if (same) {
         bool bonded = false;
         for (uint32_t k = 0; k < mydeg && !bonded; ++k) {
@@ -457,6 +465,7 @@ __global__ void __launch_bounds__(128) k_force_mx(const Dev P) {
       const float s1 = -Kn * (Rc - dn) * nvol;
       for (int c = 0; c < D; ++c) f[c] = fmaf(s1, u[c], f[c]);
       const float cfn = fabsf(s1);
+      uint32_t fr = 0;
       if (P.allow_damping || P.allow_friction) {
         double vqd[D];
         ldv<D>(P.vel_in, q, vqd);
@@ -473,12 +482,17 @@ __global__ void __launch_bounds__(128) k_force_mx(const Dev P) {
           const float tn = sqrtf(dotf<D>(tg, tg));
           if (tn > 0.f) {
             float sfr = -mu * cfn;
-            if (tn < mu * cfn * dtf / rho) sfr = -tn / rho / dtf;
+            fr = (D == 2 && (tg[1] * u[0] - tg[0] * u[1]) < 0.f) ? FR_SLIDE_NEG : FR_SLIDE;
+            if (tn < mu * cfn * dtf / rho) {
+              sfr = -tn / rho / dtf;
+              fr = FR_STICK;
+            }
             const float it = sfr / tn;
             for (int c = 0; c < D; ++c) f[c] = fmaf(it, tg[c], f[c]);
           }
         }
       }
+      if constexpr (REC) rent[nrec++] = q | (fr << 30);
     }
   }
 
@@ -489,8 +503,10 @@ __global__ void __launch_bounds__(128) k_force_mx(const Dev P) {
       double xc[D];
       ldv<D>(P.cur, d, xc);
       const double vol_i = (double)P.vol_f[d];
-      const float R = (float)in.contact_rad, Kn = (float)in.normal_stiffness;
-      const float mu = (float)in.friction_coefficient, zeta = (float)in.damping_ratio;
+      const float R = (float)in.contact_rad;
+      const float Kn = (float)(GC ? gr.kn : in.normal_stiffness);
+      const float mu = (float)(GC ? gr.mu : in.friction_coefficient);
+      const float zeta = (float)(GC ? gr.zeta : in.damping_ratio);
       const float rho = (float)gr.rho, dtf = (float)P.dt;
       constexpr int NS = 2 * D;
       const int order2[4][2] = {{3, 1}, {0, 0}, {1, 0}, {2, 1}};
@@ -500,6 +516,7 @@ __global__ void __launch_bounds__(128) k_force_mx(const Dev P) {
         const int dir = (D == 2) ? order2[k][1] : order3[k][1];
         const float dist = (float)(xc[dir] - in.wall[side]);
         if (!(fabsf(dist) <= R)) continue;
+        wbits |= 1u << (4 * k);
         const float dd = fabsf(dist);
         float Area, I;
         if constexpr (D == 2) {
@@ -532,7 +549,11 @@ __global__ void __launch_bounds__(128) k_force_mx(const Dev P) {
             const int tg = (dir + 1) % 2;
             if (fabsf(rv[tg]) > 0.f) {
               float ff = -mu * fabsf(F) * (rv[tg] > 0.f ? 1.f : -1.f);
-              if (fabsf(rv[tg]) < mu * fabsf(F) * dtf / rho) ff = -rv[tg] * rho / dtf;
+              wbits |= (rv[tg] > 0.f ? 2u : 10u) << (4 * k);
+              if (fabsf(rv[tg]) < mu * fabsf(F) * dtf / rho) {
+                ff = -rv[tg] * rho / dtf;
+                wbits |= 4u << (4 * k);
+              }
               f[tg] += ff;
               rec.a_t1 = vol_i * (double)ff;
               rec.has_fric = 1;
@@ -543,7 +564,11 @@ __global__ void __launch_bounds__(128) k_force_mx(const Dev P) {
             if (vn > 0.f) {
               const float u1 = rv[t1] / vn, u2 = rv[t2] / vn;
               float sfr = -mu * fabsf(F);
-              if (vn < mu * fabsf(F) * dtf / rho) sfr = -vn / rho / dtf;
+              wbits |= 2u << (4 * k);
+              if (vn < mu * fabsf(F) * dtf / rho) {
+                sfr = -vn / rho / dtf;
+                wbits |= 4u << (4 * k);
+              }
               f[t1] += sfr * u1;
               f[t2] += sfr * u2;
               rec.a_t1 = vol_i * (double)(sfr * u1);
@@ -621,6 +646,15 @@ __global__ void __launch_bounds__(128) k_force_mx(const Dev P) {
     stvf<D>(P.force_f, d, f);
   }
 
+  if constexpr (REC) {
+    record_masks(P, d, act, lane, rent, nrec, wbits);
+    if (P.rec_x) {
+      double xr[D];
+      if (act) ldv<D>(P.cur, d, xr);
+      record_tape<D>(P, d, act, t, xr, vpd);
+    }
+  }
+
   if (P.record_pairs) {
     for (int off = 16; off > 0; off >>= 1) {
       my_pairs += __shfl_down_sync(0xffffffffu, my_pairs, off);
@@ -636,7 +670,7 @@ __global__ void __launch_bounds__(128) k_force_mx(const Dev P) {
 
 template <int D>
 static void launch_mx(const Dev& P, const LaunchCfg& L, cudaStream_t s, uint64_t* launches, cudaEvent_t e0,
-                      cudaEvent_t e1) {
+                      cudaEvent_t e1, bool rec) {
   const uint32_t nthr = P.n_chunks * 32;
   k_predict_mx<D><<<cdiv(P.N, 256), 256, 0, s>>>(P);
   *launches += 1;
@@ -646,7 +680,16 @@ static void launch_mx(const Dev& P, const LaunchCfg& L, cudaStream_t s, uint64_t
     *launches += 1;
   }
   if (e0) cudaEventRecord(e0, s);
-  k_force_mx<D><<<cdiv(nthr, L.force_block), L.force_block, 0, s>>>(P);
+  // variants: mask recording (REC) and per-grain contact parameters (GC) are compiled in only
+  // where used, so the plain kernel keeps its register budget
+  const dim3 grid(cdiv(nthr, L.force_block)), block(L.force_block);
+  if (P.grain_contact) {
+    if (rec) k_force_mx<D, true, true><<<grid, block, 0, s>>>(P);
+    else k_force_mx<D, false, true><<<grid, block, 0, s>>>(P);
+  } else {
+    if (rec) k_force_mx<D, true, false><<<grid, block, 0, s>>>(P);
+    else k_force_mx<D, false, false><<<grid, block, 0, s>>>(P);
+  }
   if (e1) cudaEventRecord(e1, s);
   k_finalize<D><<<1, FINAL_THREADS, WREC_SMEM_CAP * sizeof(unsigned long long), s>>>(P);
   *launches += 2;
@@ -661,11 +704,11 @@ cudaError_t kernels_mixed_init() {
 }
 
 void launch_step_mixed(const Dev& P, const LaunchCfg& L, cudaStream_t s, uint64_t* launches, cudaEvent_t e0,
-                       cudaEvent_t e1) {
+                       cudaEvent_t e1, bool rec) {
   if (P.dim == 2) {
-    launch_mx<2>(P, L, s, launches, e0, e1);
+    launch_mx<2>(P, L, s, launches, e0, e1, rec);
   } else {
-    launch_mx<3>(P, L, s, launches, e0, e1);
+    launch_mx<3>(P, L, s, launches, e0, e1, rec);
   }
 }
 

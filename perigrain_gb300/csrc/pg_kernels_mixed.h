@@ -10,8 +10,9 @@
 namespace pg {
 
 cudaError_t kernels_mixed_init();
-// Enqueue one mixed-precision time step; e0/e1 (may be null) bracket the force kernel.
+// Enqueue one mixed-precision time step; e0/e1 (may be null) bracket the force kernel. With rec
+// the force kernel also records the step's contact and wall masks (Dev::rec_*).
 void launch_step_mixed(const Dev& P, const LaunchCfg& L, cudaStream_t s, uint64_t* launches,
-                       cudaEvent_t e0 = nullptr, cudaEvent_t e1 = nullptr);
+                       cudaEvent_t e0 = nullptr, cudaEvent_t e1 = nullptr, bool rec = false);
 
 }  // namespace pg

@@ -493,24 +493,32 @@ def collision_ensemble(n_inst=256, rmin=0.5e-3, rmax=1.5e-3, h=6.25e-5, seed=3, 
     return concat(out, name="collision_ensemble")
 
 
-def compaction_2d(n_grains=50, r=0.6e-3, nodes_per_grain=400, seed=4, wall_speed=-1.0, kn_power=4):
-    """Disks and squares compressed by a top wall moving at wall_speed (m/s)."""
+def compaction_2d(n_grains=50, r=0.6e-3, nodes_per_grain=400, seed=4, wall_speed=-1.0, kn_power=4, gap_frac=0.5,
+                  stir=2.0):
+    """Disks and axis-aligned squares (half side r) on a 5-column lattice whose node extents are
+    gap_frac * R_c apart, in a box whose walls sit gap_frac/2 * R_c outside the outermost nodes; the
+    top wall moves at wall_speed (m/s). Seeded grain velocities U(-stir, stir) m/s per component
+    keep every grain in contact with its neighbours during a 5000-step run."""
     rng = np.random.default_rng(seed)
-    pitch = 2 * r * 1.1
     ncol = 5
     nrow = int(math.ceil(n_grains / ncol))
-    width = ncol * pitch
-    height = nrow * pitch + 0.2 * pitch
     grains = []
     for k in range(n_grains):
         shape = "disk" if rng.integers(0, 2) == 0 else "square"
-        h = math.sqrt(shape_area(shape, r) / nodes_per_grain)
-        c = ((k % ncol + 0.5) * pitch, (k // ncol + 0.5) * pitch)
-        grains.append(make_grain(shape, r, h, c, jitter=0.1, rng=rng, angle=rng.uniform(0, math.pi / 2)))
+        rs = r if shape == "disk" else r * math.sqrt(2.0)
+        h = math.sqrt(shape_area(shape, rs) / nodes_per_grain)
+        grains.append(make_grain(shape, rs, h, (0.0, 0.0), jitter=0.1, rng=rng))
     delta = min(g.delta for g in grains)
     rc = delta / 5
+    gap = gap_frac * rc
+    ext = max(float(np.abs(g.pos).max()) for g in grains)  # largest half extent of the node sets
+    pitch = 2 * ext + gap
+    for k, g in enumerate(grains):
+        g.pos = g.pos + np.array([(k % ncol + 0.5) * pitch, (k // ncol + 0.5) * pitch])
+        g.vel[:, 0] = rng.uniform(-stir, stir)
+        g.vel[:, 1] = rng.uniform(-stir, stir)
     kn = contact_stiffness(delta, kn_power)
-    wall = [0.0, width, height, 0.0]
+    wall = [0.0, ncol * pitch, nrow * pitch, 0.0]
     speed = [0.0, 0.0, wall_speed, 0.0]
     return build_setup(grains, 2, rc, kn, 0.8, 0.9, allow_wall=1, wall=wall, wall_speed=speed, name="compaction_2d")
 
