@@ -34,7 +34,12 @@ struct AdjStep {
   double *db_o, *vb_o, *ab_o;        // [N][S] cotangent before step t
   double* pacc;                      // [N][NPARAM] parameter cotangents, accumulated per node
   const double* rbar;                // [I][2D][D] cotangent of step t's wall reactions, or null
-  int f32;                           // FP32 bond Jacobian products (mixed-precision handles)
+  double* xbb;                       // [N][S] bond share of the position cotangent (scratch)
+  double* pcb;                       // [N] bond share of the cnot cotangent (scratch)
+  // FP32 bond path (mixed-precision handles; null = FP64 bond path): the step's displacement
+  // hi/lo pairs and the FP32 force cotangents (read for step t, rewritten for step t-1)
+  const float* df;
+  float* fbf;
 };
 
 // One FP64 forward step under frozen masks (the map the adjoint differentiates).
@@ -51,6 +56,8 @@ struct ReplayStep {
 
 void launch_replay_step(const Dev& P, const ReplayStep& R, cudaStream_t s, uint64_t* launches);
 void launch_adjoint_step(const Dev& P, const AdjStep& A, cudaStream_t s, uint64_t* launches);
+// fbf from the seed cotangent (A.ab, A.vb) before the first reverse step of the FP32 bond path
+void launch_fb_init(const Dev& P, const AdjStep& A, cudaStream_t s, uint64_t* launches);
 // grad[g][k] = sum over the nodes of grain g of pacc[node][k]
 void launch_grad_reduce(const Dev& P, const double* pacc, double* grad, cudaStream_t s, uint64_t* launches);
 

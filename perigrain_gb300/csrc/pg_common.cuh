@@ -312,12 +312,15 @@ static __global__ void __launch_bounds__(FINAL_THREADS) k_finalize(const Dev P) 
     if (R > (uint32_t)WREC_SMEM_CAP || R > P.wrec_cap) {
       if (tid == 0) set_status(P.status, PG_ECAPACITY);
     } else {
+      // sort the records by (side, node in the reference's loop order); the index of the record
+      // rides in the low bits
+      double* sval = reinterpret_cast<double*>(skey + WREC_SMEM_CAP);  // [FIN_TILE][4]
       uint32_t n2 = 32;
       while (n2 < R) n2 <<= 1;
       for (uint32_t i = tid; i < n2; i += blockDim.x) {
         if (i < R) {
           const WallRec& r = P.wrec[i];
-          skey[i] = ((unsigned long long)r.gid << 32) | ((unsigned long long)r.side << 28) | i;
+          skey[i] = ((unsigned long long)r.side << 60) | ((unsigned long long)r.gid << 14) | i;
         } else {
           skey[i] = ~0ull;
         }
@@ -339,37 +342,50 @@ static __global__ void __launch_bounds__(FINAL_THREADS) k_finalize(const Dev P) 
           __syncthreads();
         }
       }
-      for (uint32_t p = tid; p < P.I * NS; p += blockDim.x) {
-        const uint32_t inst = p / NS, side = p % NS;
-        const unsigned long long lo_key = (unsigned long long)P.inst[inst].node_begin << 32;
-        const unsigned long long hi_key = (unsigned long long)P.inst[inst].node_end << 32;
-        uint32_t lo = 0, hi = R;
-        while (lo < hi) {
-          uint32_t mid = (lo + hi) >> 1;
-          if (skey[mid] < lo_key) lo = mid + 1; else hi = mid;
+      // tiles of FIN_TILE sorted records: gather their terms into shared memory in parallel, then
+      // one thread per (instance, side) subtracts its contiguous run in order (contact.h:339, :374,
+      // :411-412, :428: normal, friction, damping; terms of absent branches are stored as 0, and
+      // x - 0 == x)
+      for (uint32_t base = 0; base < R; base += FIN_TILE) {
+        const uint32_t m = min((uint32_t)FIN_TILE, R - base);
+        for (uint32_t i = tid; i < m; i += blockDim.x) {
+          const WallRec& w = P.wrec[skey[base + i] & 0x3fffu];
+          sval[4 * i + 0] = w.a_normal;
+          sval[4 * i + 1] = w.has_fric ? w.a_t1 : 0.0;
+          sval[4 * i + 2] = w.has_fric ? w.a_t2 : 0.0;
+          sval[4 * i + 3] = w.has_damp ? w.a_damp : 0.0;
         }
-        double r[3] = {0.0, 0.0, 0.0};
-        bool any = false;
-        for (uint32_t k = lo; k < R && skey[k] < hi_key; ++k) {
-          if (((skey[k] >> 28) & 0xfu) != side) continue;
-          const WallRec& w = P.wrec[skey[k] & 0x0fffffffu];
-          const int dir = (D == 2) ? ((side == 0 || side == 1) ? 0 : 1) : (int)(side % 3);
-          r[dir] = r[dir] - w.a_normal;
-          if (w.has_fric) {
-            if constexpr (D == 2) {
-              const int tg = (dir + 1) % 2;
-              r[tg] = r[tg] - w.a_t1;
-            } else {
-              r[(dir + 1) % 3] = r[(dir + 1) % 3] - w.a_t1;
-              r[(dir + 2) % 3] = r[(dir + 2) % 3] - w.a_t2;
-            }
+        __syncthreads();
+        for (uint32_t p = tid; p < P.I * NS; p += blockDim.x) {
+          const uint32_t inst = p / NS, side = p % NS;
+          const unsigned long long lo_key =
+              ((unsigned long long)side << 60) | ((unsigned long long)P.inst[inst].node_begin << 14);
+          const unsigned long long hi_key =
+              ((unsigned long long)side << 60) | ((unsigned long long)P.inst[inst].node_end << 14);
+          uint32_t lo = base, hi = base + m;
+          while (lo < hi) {
+            uint32_t mid = (lo + hi) >> 1;
+            if (skey[mid] < lo_key) lo = mid + 1; else hi = mid;
           }
-          if (w.has_damp) r[dir] = r[dir] - w.a_damp;
-          any = true;
+          if (lo >= base + m || skey[lo] >= hi_key) continue;
+          const int dir = (D == 2) ? ((side == 0 || side == 1) ? 0 : 1) : (int)(side % 3);
+          double* rp = P.reaction + ((size_t)inst * NS + side) * D;
+          double r[3] = {0.0, 0.0, 0.0};
+          for (int c = 0; c < D; ++c) r[c] = rp[c];
+          for (uint32_t k = lo; k < base + m && skey[k] < hi_key; ++k) {
+            const double* v = sval + 4 * (k - base);
+            r[dir] = r[dir] - v[0];
+            if constexpr (D == 2) {
+              r[(dir + 1) % 2] = r[(dir + 1) % 2] - v[1];
+            } else {
+              r[(dir + 1) % 3] = r[(dir + 1) % 3] - v[1];
+              r[(dir + 2) % 3] = r[(dir + 2) % 3] - v[2];
+            }
+            r[dir] = r[dir] - v[3];
+          }
+          for (int c = 0; c < D; ++c) rp[c] = r[c];
         }
-        if (any) {
-          for (int c = 0; c < D; ++c) P.reaction[((size_t)inst * NS + side) * D + c] = r[c];
-        }
+        __syncthreads();
       }
     }
   }

@@ -26,6 +26,9 @@ constexpr uint32_t NONE = 0xffffffffu;
 constexpr int MAX_CAND = 64;        // hard cap of contact candidates held per node
 constexpr int FINAL_THREADS = 1024; // threads of the per-step finalize kernel
 constexpr int WREC_SMEM_CAP = 16384;// wall-reaction records sorted in shared memory per step
+constexpr int FIN_TILE = 2048;       // sorted wall records whose terms are staged in shared memory at once
+// dynamic shared memory of k_finalize: sort keys + one tile of four terms per record
+constexpr int FINAL_SMEM = WREC_SMEM_CAP * 8 + FIN_TILE * 4 * 8;
 constexpr uint32_t ENT_NODE = 0x3fffffffu;  // partner bits of a recorded contact entry
 // friction branch of a recorded contact entry; in 2D a sliding contact also records the sign of
 // its tangential direction along perp(u) = (-u_y, u_x) (FR_SLIDE_NEG when negative)
@@ -174,6 +177,7 @@ struct Dev {
   uint32_t rec_cap;
   double *rec_x, *rec_v, *rec_w;
   uint32_t* rec_t;
+  float* rec_df;  // mixed precision: the step's displacement as FP32 hi/lo pairs (layout of bref's disp part)
   // mixed precision (PG_MIXED): FP32 hi/lo pairs (x = hi + lo to ~2^-47 |x|). `bref` interleaves,
   // per node, the pair of the FP64 displacement and the pair of the bond reference position
   // (relative to the instance's fixed origin) -- 4*SF floats, one 32-byte sector in 2D -- so a bond

@@ -107,7 +107,8 @@ static int read_status(pg_handle* h, int32_t* st) {
 // (and, when x is set, the step's tape: CurrPos, velocity, walls, step number)
 static void enqueue_rec_step(pg_handle* h, int parity, uint32_t* off, uint8_t* cnt, uint32_t* wall, uint32_t* ent,
                              uint32_t* ent_n, uint64_t cap, uint64_t* launches, double* x = nullptr,
-                             double* v = nullptr, double* w = nullptr, uint32_t* tstep = nullptr) {
+                             double* v = nullptr, double* w = nullptr, uint32_t* tstep = nullptr,
+                             float* df = nullptr) {
   Dev P = h->P;
   set_vel(h, P, parity);
   P.rec_off = off;
@@ -120,6 +121,7 @@ static void enqueue_rec_step(pg_handle* h, int parity, uint32_t* off, uint8_t* c
   P.rec_v = v;
   P.rec_w = w;
   P.rec_t = tstep;
+  P.rec_df = df;
   if (h->precision == PG_MIXED) {
     launch_step_mixed(P, h->L, h->stream, launches, nullptr, nullptr, true);
   } else {
@@ -167,11 +169,13 @@ static int ensure_tape(pg_handle* h, uint32_t C, bool masks, uint64_t ent_cap) {
     G->tape.release();
     G->off = G->wall = G->ent = G->ent_n = nullptr;
     G->cnt = nullptr;
+    G->DF = nullptr;
     G->ent_cap = 0;
     CU(G->tape.alloc(&G->X, (size_t)C * N * S));
     CU(G->tape.alloc(&G->V, (size_t)C * N * S));
     CU(G->tape.alloc(&G->W, (size_t)C * I * NS));
     CU(G->tape.alloc(&G->tstep, C));
+    if (h->precision == PG_MIXED) CU(G->tape.alloc(&G->DF, (size_t)C * N * (h->dim == 2 ? 4 : 6)));
     G->tape_steps = C;
   }
   if (masks && !G->off) {
@@ -210,8 +214,9 @@ static int enqueue_recompute(pg_handle* h, int parity, uint32_t len, uint32_t fi
       CU(cudaMemcpyAsync(V, vin, N * S * 8, cudaMemcpyDeviceToDevice, h->stream));
     } else {
       // the recording force kernel writes the tape itself
+      float* DF = G->DF ? G->DF + (size_t)i * N * (h->dim == 2 ? 4 : 6) : nullptr;
       enqueue_rec_step(h, parity, G->off + (size_t)i * N, G->cnt + (size_t)i * N, G->wall + (size_t)i * N, G->ent,
-                       G->ent_n, G->ent_cap, launches, X, V, W, G->tstep + i);
+                       G->ent_n, G->ent_cap, launches, X, V, W, G->tstep + i, DF);
     }
     parity ^= 1;
   }
@@ -253,7 +258,11 @@ static void enqueue_reverse(pg_handle* h, int cur, uint32_t len, uint32_t first_
     A.ab_o = G->cot[cur ^ 1][2];
     A.pacc = G->pacc;
     A.rbar = (with_rbar && ii == len - 1) ? G->rbar : nullptr;
-    A.f32 = (h->precision == PG_MIXED && !G->frozen) ? 1 : 0;
+    A.xbb = G->xbb;
+    A.pcb = G->pcb;
+    const bool f32 = h->precision == PG_MIXED && !G->frozen;
+    A.df = f32 ? G->DF + (size_t)ii * N * (h->dim == 2 ? 4 : 6) : nullptr;
+    A.fbf = f32 ? G->fbf : nullptr;
     launch_adjoint_step(h->P, A, h->stream, launches);
     cur ^= 1;
   }
@@ -498,6 +507,9 @@ int pg_grad_backward(pg_handle* h, const double* disp_bar, const double* vel_bar
     CU(G->mem.alloc(&G->pacc, N * NPARAM));
     CU(G->mem.alloc(&G->gradd, NG * NPARAM));
     CU(G->mem.alloc(&G->rbar, I * NS * D));
+    CU(G->mem.alloc(&G->xbb, N * S));
+    CU(G->mem.alloc(&G->pcb, N));
+    CU(G->mem.alloc(&G->fbf, N * ((D == 2) ? 2 : 4)));
   }
   uint64_t cap = G->ent_cap ? G->ent_cap : std::max<uint64_t>(1u << 20, (uint64_t)C * N / 2);
   std::vector<uint32_t> need(nseg, 0);
@@ -526,6 +538,13 @@ int pg_grad_backward(pg_handle* h, const double* disp_bar, const double* vel_bar
     CU(cudaMemsetAsync(h->P.status, 0, 4, h->stream));
     uint64_t launches = 0;
     CU(cudaEventRecord(G->e0, h->stream));
+    if (h->precision == PG_MIXED && !G->frozen) {
+      AdjStep A{};
+      A.ab = G->cot[0][2];
+      A.vb = G->cot[0][1];
+      A.fbf = G->fbf;
+      launch_fb_init(h->P, A, h->stream, &launches);
+    }
     int cur = 0;
     for (uint32_t k = nseg; k-- > 0;) {
       const uint32_t len = std::min(C, T - k * C);

@@ -78,6 +78,7 @@ struct GradState {
   // segment tape (C steps)
   uint32_t tape_steps = 0;
   double *X = nullptr, *V = nullptr, *W = nullptr;
+  float* DF = nullptr;  // mixed precision: displacement hi/lo pairs per step
   uint32_t* tstep = nullptr;
   uint32_t *off = nullptr, *wall = nullptr, *ent = nullptr, *ent_n = nullptr;
   uint8_t* cnt = nullptr;
@@ -85,6 +86,8 @@ struct GradState {
   // cotangents and parameter accumulators
   double* cot[2][3] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};
   double *pacc = nullptr, *gradd = nullptr, *rbar = nullptr, *wall_out = nullptr;
+  double *xbb = nullptr, *pcb = nullptr;
+  float* fbf = nullptr;
   // graphs of one full segment: recording (per velocity parity) and reverse (per cotangent slot)
   cudaGraphExec_t g_rec[2] = {nullptr, nullptr};
   cudaGraphExec_t g_adj[2] = {nullptr, nullptr};

@@ -516,16 +516,14 @@ static void launch_step_t(const Dev& P, const LaunchCfg& L, cudaStream_t s, uint
     else k_force<D, false, false><<<grid, block, 0, s>>>(P);
   }
   if (e1) cudaEventRecord(e1, s);
-  k_finalize<D><<<1, FINAL_THREADS, WREC_SMEM_CAP * sizeof(unsigned long long), s>>>(P);
+  k_finalize<D><<<1, FINAL_THREADS, FINAL_SMEM, s>>>(P);
   *launches += 2;
 }
 
 cudaError_t kernels_init() {
-  cudaError_t e = cudaFuncSetAttribute(k_finalize<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       WREC_SMEM_CAP * (int)sizeof(unsigned long long));
+  cudaError_t e = cudaFuncSetAttribute(k_finalize<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, FINAL_SMEM);
   if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(k_finalize<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              WREC_SMEM_CAP * (int)sizeof(unsigned long long));
+  return cudaFuncSetAttribute(k_finalize<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, FINAL_SMEM);
 }
 
 void launch_step(const Dev& P, const LaunchCfg& L, cudaStream_t s, uint64_t* launches, bool rec) {

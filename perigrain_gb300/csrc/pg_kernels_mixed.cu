@@ -318,6 +318,18 @@ __global__ void __launch_bounds__(128) k_force_mx(const Dev P) {
     // neighbour gathers issued before either is used
     float dh[D], dl[D], xh[D], xl[D];
     if (mov) ld_ref<D>(P.bref, P.N, d, dh, dl, xh, xl);
+    if constexpr (REC) {
+      if (mov && P.rec_df) {
+        if constexpr (D == 2) {
+          reinterpret_cast<float4*>(P.rec_df)[d] = make_float4(dh[0], dh[1], dl[0], dl[1]);
+        } else {
+          for (int c = 0; c < D; ++c) {
+            P.rec_df[(size_t)c * P.N + d] = dh[c];
+            P.rec_df[(size_t)(D + c) * P.N + d] = dl[c];
+          }
+        }
+      }
+    }
     for (uint32_t k = 0; k < cdeg; k += 2) {
       const bool two = (k + 1) < cdeg;
       const uint32_t wa = P.alive[w0 + k];
@@ -691,16 +703,14 @@ static void launch_mx(const Dev& P, const LaunchCfg& L, cudaStream_t s, uint64_t
     else k_force_mx<D, false, false><<<grid, block, 0, s>>>(P);
   }
   if (e1) cudaEventRecord(e1, s);
-  k_finalize<D><<<1, FINAL_THREADS, WREC_SMEM_CAP * sizeof(unsigned long long), s>>>(P);
+  k_finalize<D><<<1, FINAL_THREADS, FINAL_SMEM, s>>>(P);
   *launches += 2;
 }
 
 cudaError_t kernels_mixed_init() {
-  cudaError_t e = cudaFuncSetAttribute(k_finalize<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       WREC_SMEM_CAP * (int)sizeof(unsigned long long));
+  cudaError_t e = cudaFuncSetAttribute(k_finalize<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, FINAL_SMEM);
   if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(k_finalize<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              WREC_SMEM_CAP * (int)sizeof(unsigned long long));
+  return cudaFuncSetAttribute(k_finalize<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, FINAL_SMEM);
 }
 
 void launch_step_mixed(const Dev& P, const LaunchCfg& L, cudaStream_t s, uint64_t* launches, cudaEvent_t e0,
