@@ -262,6 +262,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=400)
     ap.add_argument("--no-adjoint", action="store_true", help="skip the gradient-path measurement")
+    ap.add_argument("--profile-adjoint", type=int, default=0, metavar="STEPS",
+                    help="only a forward + backward of STEPS steps of the differentiable compaction "
+                         "(checkpoint every 100; the command profiled under ncu)")
     ap.add_argument("--profile-run", action="store_true",
                     help="only warmup + steps of the engine (the command profiled under ncu)")
     a = ap.parse_args()
@@ -288,6 +291,18 @@ def main():
 
     import perigrain_gb300 as pg
     from perigrain_gb300 import Simulation
+
+    if a.profile_adjoint:
+        from perigrain_gb300 import grad, setups
+
+        s = setups.workload(4)
+        sim = Simulation(s, dt=setups.WORKLOADS[4]["dt"], precision=a.precision)
+        run = grad.GradRun(sim, a.profile_adjoint, checkpoint_every=100)
+        r, ke = run.forward()
+        g = run.backward(ke_bar=1.0 / ke)
+        print("profile adjoint: compaction_2d, %d nodes, %d steps, %s, finite %s"
+              % (s.n_nodes, a.profile_adjoint, run.times(), bool(np.isfinite(g).all())))
+        return
 
     pg.engine.select_device(local_rank)
     dist = None

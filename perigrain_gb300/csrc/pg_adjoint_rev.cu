@@ -16,8 +16,8 @@
 // slot, as in the force kernels), partial sums added in shared memory in a fixed order; its bond
 // products run in FP32 for mixed-precision handles (GB300 runs FP64 at a small fraction of its
 // FP32 rate) and in FP64 for FP64 handles and frozen replays (the FP64 reference gradient).
-// k_adj_rest: one thread per node for contacts, walls and the integrator, FP64; the cotangent
-// state is FP64 throughout.
+// k_adj_rest: same chunk x SUB-warp split for contacts (entries round-robin over the warps),
+// walls and the integrator, FP64; the cotangent state is FP64 throughout.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -328,20 +328,189 @@ __global__ void __launch_bounds__(32 * SUB) k_adj_bonds(const Dev P, const AdjSt
   A.pcb[d] = pcs;
 }
 
-// Contact, wall and integrator part of the reverse step (one thread per node); adds the bond
-// share from k_adj_bonds and, for the FP32 bond path, writes the force cotangent of the next
-// reverse step to fbf.
+// Contact, wall and integrator part of the reverse step: one block per 32-node chunk, SUB warps;
+// warp w takes the node's contact entries i = w, w+SUB, ..., warp 0 also the walls; the partial
+// cotangents are summed in shared memory in a fixed order and warp 0 adds the bond share from
+// k_adj_bonds and runs the integrator. For the FP32 bond path it also writes the force cotangent
+// of the next reverse step to fbf.
 template <int D>
-__global__ void __launch_bounds__(128) k_adj_rest(const Dev P, const AdjStep A) {
+__global__ void __launch_bounds__(32 * SUB) k_adj_rest(const Dev P, const AdjStep A) {
   constexpr int NS = 2 * D;
-  const uint32_t d = blockIdx.x * blockDim.x + threadIdx.x;
-  if (d >= P.N) return;
+  constexpr int NV = 2 * D + NPARAM;  // xb[D], vfb[D], pc[NPARAM]
+  __shared__ double red[SUB][NV][32];
+  const uint32_t lane = threadIdx.x & 31, sub = threadIdx.x >> 5;
+  const uint32_t d = blockIdx.x * 32 + lane;
+  const bool act = d < P.N;
+  double acc[NV];
+  for (int v = 0; v < NV; ++v) acc[v] = 0.0;
+  double* xb = acc;
+  double* vfb = acc + D;
+  double* pc = acc + 2 * D;
   double Fb[D];
-  const uint32_t g = P.node_grain[d];
-  double zero[D];
-  for (int c = 0; c < D; ++c) zero[c] = 0.0;
-  if (!force_bar<D>(P, A, d, Fb)) {
+  uint32_t g = 0;
+  bool live = false;
+  if (act) {
+    g = P.node_grain[d];
+    live = force_bar<D>(P, A, d, Fb);
+  }
+  if (live) {
+    const GrainDev gr = P.grain[g];
+    const InstDev& in = P.inst[gr.inst];
+    double xp[D], vp[D];
+    ldv<D>(A.X, d, xp);
+    ldv<D>(A.V, d, vp);
+    const double volp = P.vol[d];
+
+    // contacts: the node's own forces (its list) and the partners' forces from it (their lists)
+    const bool damp = P.allow_damping, fric = P.allow_friction;
+    const uint32_t o = A.off[d], n = A.cnt[d];
+    for (uint32_t i = sub; i < n; i += SUB) {
+      const uint32_t e = A.ent[o + i];
+      const uint32_t q = e & ENT_NODE, fr = e >> 30;
+      const uint32_t gqi = P.node_grain[q];
+      const bool same = gqi == g;
+      const GrainDev gq = P.grain[gqi];
+      double Kn, Rc, zeta, mu;
+      pair_params<D>(P, in, gr, gq, same, d, q, &Kn, &Rc, &zeta, &mu);
+      double xq[D], vq[D], y[D], r[D];
+      ldv<D>(A.X, q, xq);
+      ldv<D>(A.V, q, vq);
+      for (int c = 0; c < D; ++c) {
+        y[c] = xq[c] - xp[c];
+        r[c] = vp[c] - vq[c];
+      }
+      double yb[D], rb[D], pb[3] = {0.0, 0.0, 0.0};
+      for (int c = 0; c < D; ++c) {
+        yb[c] = 0.0;
+        rb[c] = 0.0;
+      }
+      pair_vjp<D>(y, r, Fb, Kn, Rc, zeta, mu, P.vol[q], gr.rho, fr, damp, fric, P.dt, yb, rb, pb);
+      for (int c = 0; c < D; ++c) {
+        xb[c] -= yb[c];
+        vfb[c] += rb[c];
+      }
+      if (same) {
+        pc[0] += pb[0] / Rc;  // K_n' = cnot / R_c'
+        pc[2] += pb[1];
+        pc[3] += pb[2];
+      } else {
+        pc[1] += 0.5 * pb[0];
+        pc[2] += 0.5 * pb[1];
+        pc[3] += 0.5 * pb[2];
+      }
+      // the partner's force from this node, if the partner recorded it
+      const uint32_t oq = A.off[q], nq = A.cnt[q];
+      uint32_t frq = 4u;
+      for (uint32_t k = 0; k < nq; ++k) {
+        const uint32_t eq = A.ent[oq + k];
+        if ((eq & ENT_NODE) == d) {
+          frq = eq >> 30;
+          break;
+        }
+      }
+      if (frq == 4u) continue;
+      double Fq[D];
+      if (!force_bar<D>(P, A, q, Fq)) continue;
+      double y2[D], r2[D], yb2[D], rb2[D], pb2[3] = {0.0, 0.0, 0.0};
+      for (int c = 0; c < D; ++c) {
+        y2[c] = xp[c] - xq[c];
+        r2[c] = vq[c] - vp[c];
+        yb2[c] = 0.0;
+        rb2[c] = 0.0;
+      }
+      pair_vjp<D>(y2, r2, Fq, Kn, Rc, zeta, mu, volp, gq.rho, frq, damp, fric, P.dt, yb2, rb2, pb2);
+      for (int c = 0; c < D; ++c) {
+        xb[c] += yb2[c];
+        vfb[c] -= rb2[c];
+      }
+      if (!same) {
+        pc[1] += 0.5 * pb2[0];
+        pc[2] += 0.5 * pb2[1];
+        pc[3] += 0.5 * pb2[2];
+      }
+    }
+
+    // walls: the node's force and, at the objective's step, its share of the wall reactions
+    const uint32_t wbits = A.wall[d];
+    if (sub == 0 && wbits) {
+      const double R = in.contact_rad, Kn = gr.kn, rho = gr.rho;
+      for (int k = 0; k < NS; ++k) {
+        if (!wb_contact(wbits, k)) continue;
+        int side, dir;
+        wall_side<D>(k, &side, &dir);
+        double gv[D];
+        for (int c = 0; c < D; ++c) gv[c] = Fb[c];
+        if (A.rbar) {
+          // reaction[side] -= vol_p * (the node's wall force of this side)
+          for (int c = 0; c < D; ++c) gv[c] -= volp * A.rbar[((size_t)gr.inst * NS + side) * D + c];
+        }
+        const double dist = xp[dir] - A.W[(size_t)gr.inst * NS + side];
+        const double dd = fmin(fabs(dist), R);  // the replay's extension beyond R
+        const double cs = dist > 0 ? 1.0 : -1.0;
+        double Ar, Ap, FK, FKp;
+        wall_geom<D>(R, dd, &Ar, &Ap, &FK, &FKp);
+        const double F = Kn * FK, Fp = Kn * FKp;  // dF/d(dd); d(dd)/dX = cs
+        // normal: f[dir] += cs F
+        xb[dir] += gv[dir] * Fp;
+        pc[1] += gv[dir] * cs * FK;
+        double rv[D];
+        for (int c = 0; c < D; ++c) rv[c] = vp[c];
+        rv[dir] -= in.wall_speed[side];
+        if (fric && wb_fric(wbits, k)) {
+          const bool stick = wb_stick(wbits, k);
+          const double sF = F > 0 ? 1.0 : (F < 0 ? -1.0 : 0.0);
+          if constexpr (D == 2) {
+            const int tg = (dir + 1) % 2;
+            if (stick) {
+              vfb[tg] += gv[tg] * (-rho / P.dt);
+            } else {
+              const double vts = wb_neg(wbits, k) ? -1.0 : 1.0;
+              xb[dir] += gv[tg] * (-gr.mu * vts * sF * Fp * cs);
+              pc[3] += gv[tg] * (-fabs(F) * vts);
+              pc[1] += gv[tg] * (-gr.mu * vts * sF * FK);
+            }
+          } else {
+            const int t1 = (dir + 1) % 3, t2 = (dir + 2) % 3;
+            if (stick) {
+              vfb[t1] += gv[t1] * (-1.0 / (rho * P.dt));
+              vfb[t2] += gv[t2] * (-1.0 / (rho * P.dt));
+            } else {
+              const double v1 = rv[t1], v2 = rv[t2];
+              const double vn = sqrt(v1 * v1 + v2 * v2);
+              if (vn > 0) {
+                const double u1 = v1 / vn, u2 = v2 / vn;
+                const double a = gv[t1] * u1 + gv[t2] * u2;
+                xb[dir] += -gr.mu * a * sF * Fp * cs;
+                pc[3] += -fabs(F) * a;
+                pc[1] += -gr.mu * a * sF * FK;
+                vfb[t1] += -gr.mu * fabs(F) * (gv[t1] - a * u1) / vn;
+                vfb[t2] += -gr.mu * fabs(F) * (gv[t2] - a * u2) / vn;
+              }
+            }
+          }
+        }
+        if (damp) {
+          // df = -dc rv[dir], dc = 2 zeta sqrt(K_n rho) sqrt(|Area|)
+          const double sq = sqrt(Kn * rho);
+          const double sa = sqrt(fabs(Ar));
+          const double dc = 2.0 * gr.zeta * sq * sa;
+          vfb[dir] += gv[dir] * (-dc);
+          if (sa > 0) xb[dir] += gv[dir] * (-rv[dir]) * gr.zeta * sq * (Ap / sa) * cs;
+          pc[2] += gv[dir] * (-rv[dir]) * 2.0 * sq * sa;
+          if (Kn != 0.0) pc[1] += gv[dir] * (-rv[dir]) * dc / (2.0 * Kn);
+        }
+      }
+    }
+  }
+
+  // fixed-order sum of the SUB partial cotangents, then the integrator (warp 0)
+  for (int v = 0; v < NV; ++v) red[sub][v][lane] = acc[v];
+  __syncthreads();
+  if (sub != 0 || !act) return;
+  if (!live) {
     // the state of this node does not depend on the parameters
+    double zero[D];
+    for (int c = 0; c < D; ++c) zero[c] = 0.0;
     stv<D>(A.db_o, d, zero);
     stv<D>(A.vb_o, d, zero);
     stv<D>(A.ab_o, d, zero);
@@ -352,158 +521,16 @@ __global__ void __launch_bounds__(128) k_adj_rest(const Dev P, const AdjStep A) 
     }
     return;
   }
-  const GrainDev gr = P.grain[g];
-  const InstDev& in = P.inst[gr.inst];
-  double xb[D], vfb[D], pc[NPARAM];
-  ldv<D>(A.xbb, d, xb);
-  for (int c = 0; c < D; ++c) vfb[c] = 0.0;
-  pc[0] = A.pcb[d];
-  for (int k = 1; k < NPARAM; ++k) pc[k] = 0.0;
-  double xp[D], vp[D];
-  ldv<D>(A.X, d, xp);
-  ldv<D>(A.V, d, vp);
-  const double volp = P.vol[d];
-
-  // contacts: the node's own forces (its list) and the partners' forces from it (their lists)
-  const bool damp = P.allow_damping, fric = P.allow_friction;
-  const uint32_t o = A.off[d], n = A.cnt[d];
-  for (uint32_t i = 0; i < n; ++i) {
-    const uint32_t e = A.ent[o + i];
-    const uint32_t q = e & ENT_NODE, fr = e >> 30;
-    const uint32_t gqi = P.node_grain[q];
-    const bool same = gqi == g;
-    const GrainDev gq = P.grain[gqi];
-    double Kn, Rc, zeta, mu;
-    pair_params<D>(P, in, gr, gq, same, d, q, &Kn, &Rc, &zeta, &mu);
-    double xq[D], vq[D], y[D], r[D];
-    ldv<D>(A.X, q, xq);
-    ldv<D>(A.V, q, vq);
-    for (int c = 0; c < D; ++c) {
-      y[c] = xq[c] - xp[c];
-      r[c] = vp[c] - vq[c];
-    }
-    double yb[D], rb[D], pb[3] = {0.0, 0.0, 0.0};
-    for (int c = 0; c < D; ++c) {
-      yb[c] = 0.0;
-      rb[c] = 0.0;
-    }
-    pair_vjp<D>(y, r, Fb, Kn, Rc, zeta, mu, P.vol[q], gr.rho, fr, damp, fric, P.dt, yb, rb, pb);
-    for (int c = 0; c < D; ++c) {
-      xb[c] -= yb[c];
-      vfb[c] += rb[c];
-    }
-    if (same) {
-      pc[0] += pb[0] / Rc;  // K_n' = cnot / R_c'
-      pc[2] += pb[1];
-      pc[3] += pb[2];
-    } else {
-      pc[1] += 0.5 * pb[0];
-      pc[2] += 0.5 * pb[1];
-      pc[3] += 0.5 * pb[2];
-    }
-    // the partner's force from this node, if the partner recorded it
-    const uint32_t oq = A.off[q], nq = A.cnt[q];
-    uint32_t frq = 4u;
-    for (uint32_t k = 0; k < nq; ++k) {
-      const uint32_t eq = A.ent[oq + k];
-      if ((eq & ENT_NODE) == d) {
-        frq = eq >> 30;
-        break;
-      }
-    }
-    if (frq == 4u) continue;
-    double Fq[D];
-    if (!force_bar<D>(P, A, q, Fq)) continue;
-    double y2[D], r2[D], yb2[D], rb2[D], pb2[3] = {0.0, 0.0, 0.0};
-    for (int c = 0; c < D; ++c) {
-      y2[c] = xp[c] - xq[c];
-      r2[c] = vq[c] - vp[c];
-      yb2[c] = 0.0;
-      rb2[c] = 0.0;
-    }
-    pair_vjp<D>(y2, r2, Fq, Kn, Rc, zeta, mu, volp, gq.rho, frq, damp, fric, P.dt, yb2, rb2, pb2);
-    for (int c = 0; c < D; ++c) {
-      xb[c] += yb2[c];
-      vfb[c] -= rb2[c];
-    }
-    if (!same) {
-      pc[1] += 0.5 * pb2[0];
-      pc[2] += 0.5 * pb2[1];
-      pc[3] += 0.5 * pb2[2];
-    }
+  for (int v = 0; v < NV; ++v) {
+    double sm = red[0][v][lane];
+    for (int w = 1; w < SUB; ++w) sm += red[w][v][lane];
+    acc[v] = sm;
   }
-
-  // walls: the node's force and, at the objective's step, its share of the wall reactions
-  const uint32_t wbits = A.wall[d];
-  if (wbits) {
-    const double R = in.contact_rad, Kn = gr.kn, rho = gr.rho;
-    for (int k = 0; k < NS; ++k) {
-      if (!wb_contact(wbits, k)) continue;
-      int side, dir;
-      wall_side<D>(k, &side, &dir);
-      double gv[D];
-      for (int c = 0; c < D; ++c) gv[c] = Fb[c];
-      if (A.rbar) {
-        // reaction[side] -= vol_p * (the node's wall force of this side)
-        for (int c = 0; c < D; ++c) gv[c] -= volp * A.rbar[((size_t)gr.inst * NS + side) * D + c];
-      }
-      const double dist = xp[dir] - A.W[(size_t)gr.inst * NS + side];
-      const double dd = fmin(fabs(dist), R);  // the replay's extension beyond R
-      const double cs = dist > 0 ? 1.0 : -1.0;
-      double Ar, Ap, FK, FKp;
-      wall_geom<D>(R, dd, &Ar, &Ap, &FK, &FKp);
-      const double F = Kn * FK, Fp = Kn * FKp;  // dF/d(dd); d(dd)/dX = cs
-      // normal: f[dir] += cs F
-      xb[dir] += gv[dir] * Fp;
-      pc[1] += gv[dir] * cs * FK;
-      double rv[D];
-      for (int c = 0; c < D; ++c) rv[c] = vp[c];
-      rv[dir] -= in.wall_speed[side];
-      if (fric && wb_fric(wbits, k)) {
-        const bool stick = wb_stick(wbits, k);
-        const double sF = F > 0 ? 1.0 : (F < 0 ? -1.0 : 0.0);
-        if constexpr (D == 2) {
-          const int tg = (dir + 1) % 2;
-          if (stick) {
-            vfb[tg] += gv[tg] * (-rho / P.dt);
-          } else {
-            const double vts = wb_neg(wbits, k) ? -1.0 : 1.0;
-            xb[dir] += gv[tg] * (-gr.mu * vts * sF * Fp * cs);
-            pc[3] += gv[tg] * (-fabs(F) * vts);
-            pc[1] += gv[tg] * (-gr.mu * vts * sF * FK);
-          }
-        } else {
-          const int t1 = (dir + 1) % 3, t2 = (dir + 2) % 3;
-          if (stick) {
-            vfb[t1] += gv[t1] * (-1.0 / (rho * P.dt));
-            vfb[t2] += gv[t2] * (-1.0 / (rho * P.dt));
-          } else {
-            const double v1 = rv[t1], v2 = rv[t2];
-            const double vn = sqrt(v1 * v1 + v2 * v2);
-            if (vn > 0) {
-              const double u1 = v1 / vn, u2 = v2 / vn;
-              const double a = gv[t1] * u1 + gv[t2] * u2;
-              xb[dir] += -gr.mu * a * sF * Fp * cs;
-              pc[3] += -fabs(F) * a;
-              pc[1] += -gr.mu * a * sF * FK;
-              vfb[t1] += -gr.mu * fabs(F) * (gv[t1] - a * u1) / vn;
-              vfb[t2] += -gr.mu * fabs(F) * (gv[t2] - a * u2) / vn;
-            }
-          }
-        }
-      }
-      if (damp) {
-        // df = -dc rv[dir], dc = 2 zeta sqrt(K_n rho) sqrt(|Area|)
-        const double sq = sqrt(Kn * rho);
-        const double sa = sqrt(fabs(Ar));
-        const double dc = 2.0 * gr.zeta * sq * sa;
-        vfb[dir] += gv[dir] * (-dc);
-        if (sa > 0) xb[dir] += gv[dir] * (-rv[dir]) * gr.zeta * sq * (Ap / sa) * cs;
-        pc[2] += gv[dir] * (-rv[dir]) * 2.0 * sq * sa;
-        if (Kn != 0.0) pc[1] += gv[dir] * (-rv[dir]) * dc / (2.0 * Kn);
-      }
-    }
-  }
+  double xbond[D];
+  ldv<D>(A.xbb, d, xbond);
+  for (int c = 0; c < D; ++c) xb[c] += xbond[c];
+  pc[0] += A.pcb[d];
+  const GrainDev& gr = P.grain[g];
 
   // integrator
   double db[D], vb[D], o1[D], o2[D], o3[D];
@@ -559,15 +586,14 @@ __global__ void __launch_bounds__(256) k_grad_reduce(const Dev P, const double* 
 }
 
 void launch_adjoint_step(const Dev& P, const AdjStep& A, cudaStream_t s, uint64_t* launches) {
-  const uint32_t nb = (P.N + 127) / 128;
   if (P.dim == 2) {
     if (A.fbf) k_adj_bonds<2, true><<<P.n_chunks, 32 * SUB, 0, s>>>(P, A);
     else k_adj_bonds<2, false><<<P.n_chunks, 32 * SUB, 0, s>>>(P, A);
-    k_adj_rest<2><<<nb, 128, 0, s>>>(P, A);
+    k_adj_rest<2><<<P.n_chunks, 32 * SUB, 0, s>>>(P, A);
   } else {
     if (A.fbf) k_adj_bonds<3, true><<<P.n_chunks, 32 * SUB, 0, s>>>(P, A);
     else k_adj_bonds<3, false><<<P.n_chunks, 32 * SUB, 0, s>>>(P, A);
-    k_adj_rest<3><<<nb, 128, 0, s>>>(P, A);
+    k_adj_rest<3><<<P.n_chunks, 32 * SUB, 0, s>>>(P, A);
   }
   *launches += 2;
 }

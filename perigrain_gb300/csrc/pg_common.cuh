@@ -367,12 +367,18 @@ static __global__ void __launch_bounds__(FINAL_THREADS) k_finalize(const Dev P) 
             uint32_t mid = (lo + hi) >> 1;
             if (skey[mid] < lo_key) lo = mid + 1; else hi = mid;
           }
-          if (lo >= base + m || skey[lo] >= hi_key) continue;
+          uint32_t end = lo, top = base + m;
+          while (end < top) {
+            uint32_t mid = (end + top) >> 1;
+            if (skey[mid] < hi_key) end = mid + 1; else top = mid;
+          }
+          if (end == lo) continue;
           const int dir = (D == 2) ? ((side == 0 || side == 1) ? 0 : 1) : (int)(side % 3);
           double* rp = P.reaction + ((size_t)inst * NS + side) * D;
           double r[3] = {0.0, 0.0, 0.0};
           for (int c = 0; c < D; ++c) r[c] = rp[c];
-          for (uint32_t k = lo; k < base + m && skey[k] < hi_key; ++k) {
+#pragma unroll 4
+          for (uint32_t k = lo; k < end; ++k) {
             const double* v = sval + 4 * (k - base);
             r[dir] = r[dir] - v[0];
             if constexpr (D == 2) {
