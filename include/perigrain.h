@@ -188,6 +188,24 @@ int pg_get_launch_count(pg_handle* h, uint64_t* launches);
 int pg_set_timing(pg_handle* h, int32_t enable);
 int pg_get_kernel_times(pg_handle* h, double* force_ms, double* total_ms, uint64_t* force_launches);
 
+/* ---- post-processing on the device ---------------------------------------------------------- */
+/* The quantities the reference's post-processing scripts compute from the tc_/wall_ files
+ * (read_sim_output.py:126-133, :183-232, :305-312; gen_damage_data.py; gen_timestep_data.py),
+ * computed from the current state on the device; only the aggregates are copied out. Every
+ * pointer may be NULL (not computed). Grain means are over the grain's nodes (numpy `mean(axis=0)`);
+ * damage of a node is (deg0 - deg) / deg0 with deg the intact bonds now and deg0 at creation. */
+typedef struct pg_post {
+  double* grain_mean_vel;     /* [n_grains*dim] particle_mean_vel */
+  double* grain_mean_acc;     /* [n_grains*dim] particle_mean_acc */
+  double* grain_mean_currpos; /* [n_grains*dim] particle_mean_CurrPos */
+  double* grain_force;        /* [n_grains*dim] particle_force: sum of the force density */
+  double* grain_damage;       /* [n_grains] mean node damage of the grain */
+  double* node_damage;        /* [n_nodes] node damage (the `damage` plot quantity) */
+  double* inertial_force;     /* [n_instances*dim] sum of vol * rho * acc (read_force_val f_sum) */
+  double* volume_fraction;    /* [n_instances] grain volume / wall box volume (extract_bulk) */
+} pg_post;
+int pg_postprocess(pg_handle* h, const pg_post* out);
+
 /* ---- gradients ------------------------------------------------------------------------------ */
 /* The reference has no gradient path; these entry points differentiate its time step
  * (timeloop.h:608-879, the run_timeloop body) with respect to per-grain parameters.

@@ -68,6 +68,11 @@ CONF_FIELDS = [
 ]
 
 
+class Post(C.Structure):
+    _fields_ = [(k, f64p) for k in ("grain_mean_vel", "grain_mean_acc", "grain_mean_currpos", "grain_force",
+                                    "grain_damage", "node_damage", "inertial_force", "volume_fraction")]
+
+
 class Conf(C.Structure):
     _fields_ = CONF_FIELDS
 
@@ -107,6 +112,7 @@ PROTOTYPES = [
     ("pg_build_bonds_noalloc", C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_double, C.c_void_p, C.c_uint64,
                                          u64p, C.c_void_p]),
     ("pg_noalloc_last_error", C.c_char_p, []),
+    ("pg_postprocess", C.c_int, [C.c_void_p, C.c_void_p]),
     # gradients
     ("pg_set_grain_params", C.c_int, [C.c_void_p, f64p, f64p, f64p, f64p, f64p]),
     ("pg_get_grain_params", C.c_int, [C.c_void_p, f64p, f64p, f64p, f64p, f64p]),

@@ -144,6 +144,9 @@ struct pg_handle {
   cudaEvent_t ev_t0 = nullptr, ev_t1 = nullptr;
   // gradient path
   std::unique_ptr<GradState> grad;
+  // post-processing scratch (pg_postprocess)
+  double* post_sum = nullptr;
+  double* post_damage = nullptr;
 
   ~pg_handle() {
     if (stream) cudaStreamSynchronize(stream);

@@ -6,6 +6,7 @@
 #include <algorithm>
 #include <cctype>
 #include <chrono>
+#include <cstdlib>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -755,6 +756,12 @@ extern "C" int pg_run_simulation(const char* root_c, uint32_t dim, int32_t preci
 
   auto start_time = std::chrono::system_clock::now();
   std::vector<double> run_time, t_ind;
+  // PERIGRAIN_TIMESTEP_DATA=1: the time series gen_timestep_data.py / gen_damage_data.py /
+  // gen_wall_reaction.py build from the output files, computed on the device at each output
+  const char* tsd_env = std::getenv("PERIGRAIN_TIMESTEP_DATA");
+  const bool tsd = tsd_env && *tsd_env && std::string(tsd_env) != "0";
+  const uint32_t NSd = 2 * dim;
+  std::vector<double> ts_time, ts_wall, ts_react, ts_phi, ts_dmg, ts_force, ts_vel, ts_acc, ts_pos, ts_fsum;
   const uint32_t T = C.timesteps;
   uint64_t too_close_seen = 0;
   uint32_t t = 1;
@@ -806,6 +813,31 @@ extern "C" int pg_run_simulation(const char* root_c, uint32_t dim, int32_t preci
       pg_get_device_status(H, nullptr, &tc);
       for (; too_close_seen < tc; ++too_close_seen) std::cout << "Error: nodes too close" << std::endl;
       if ((rc = pg_write_snapshot(H, S, out.c_str(), counter))) return rc;
+      if (tsd) {
+        const uint32_t G = S->G;
+        std::vector<double> v((size_t)G * dim), a(v.size()), x(v.size()), f(v.size()), dmg(G), fs(dim), phi(1),
+            wl(NSd), re((size_t)NSd * dim);
+        pg_post po{};
+        po.grain_mean_vel = v.data();
+        po.grain_mean_acc = a.data();
+        po.grain_mean_currpos = x.data();
+        po.grain_force = f.data();
+        po.grain_damage = dmg.data();
+        po.inertial_force = fs.data();
+        po.volume_fraction = phi.data();
+        if ((rc = pg_postprocess(H, &po)) || (rc = pg_get_wall(H, wl.data())) || (rc = pg_get_reaction(H, re.data())))
+          return iofail(rc, pg_last_error());
+        ts_time.push_back((double)counter * C.dt * (double)C.modulo);  // extract_bulk: t * dt * modulo
+        ts_wall.insert(ts_wall.end(), wl.begin(), wl.end());
+        ts_react.insert(ts_react.end(), re.begin(), re.end());
+        ts_phi.push_back(phi[0]);
+        ts_dmg.insert(ts_dmg.end(), dmg.begin(), dmg.end());
+        ts_force.insert(ts_force.end(), f.begin(), f.end());
+        ts_vel.insert(ts_vel.end(), v.begin(), v.end());
+        ts_acc.insert(ts_acc.end(), a.begin(), a.end());
+        ts_pos.insert(ts_pos.end(), x.begin(), x.end());
+        ts_fsum.insert(ts_fsum.end(), fs.begin(), fs.end());
+      }
       auto stop_time = std::chrono::system_clock::now();
       auto duration = std::chrono::duration_cast<std::chrono::milliseconds>(stop_time - start_time);
       start_time = stop_time;
@@ -836,6 +868,23 @@ extern "C" int pg_run_simulation(const char* root_c, uint32_t dim, int32_t preci
     w.add_dataset("run_time", h5l::DType::F64, {run_time.size(), 1}, run_time.data());
     w.add_dataset("t_ind", h5l::DType::F64, {t_ind.size(), 1}, t_ind.data());
     if (!w.write(out + "/run_time.h5")) return iofail(PG_EIO, "cannot write run_time.h5");
+  }
+  if (tsd) {
+    // one row per output step, field names of gen_timestep_data.py (plus the damage and f_sum of
+    // gen_damage_data.py / read_force_val)
+    h5l::Writer w;
+    const uint64_t T = ts_time.size(), G = S->G;
+    w.add_dataset("time", h5l::DType::F64, {T}, ts_time.data());
+    w.add_dataset("wall_loc", h5l::DType::F64, {T, NSd}, ts_wall.data());
+    w.add_dataset("wall_force", h5l::DType::F64, {T, NSd, dim}, ts_react.data());
+    w.add_dataset("volume_fraction", h5l::DType::F64, {T}, ts_phi.data());
+    w.add_dataset("particle_damage", h5l::DType::F64, {T, G}, ts_dmg.data());
+    w.add_dataset("particle_force", h5l::DType::F64, {T, G, dim}, ts_force.data());
+    w.add_dataset("particle_mean_vel", h5l::DType::F64, {T, G, dim}, ts_vel.data());
+    w.add_dataset("particle_mean_acc", h5l::DType::F64, {T, G, dim}, ts_acc.data());
+    w.add_dataset("particle_mean_CurrPos", h5l::DType::F64, {T, G, dim}, ts_pos.data());
+    w.add_dataset("f_sum", h5l::DType::F64, {T, dim}, ts_fsum.data());
+    if (!w.write(out + "/timestep_data.h5")) return iofail(PG_EIO, "cannot write timestep_data.h5");
   }
   auto stop_all = std::chrono::system_clock::now();
   std::cout << "Runtime: " << std::chrono::duration_cast<std::chrono::seconds>(stop_all - start_all).count()

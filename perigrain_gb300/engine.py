@@ -124,6 +124,22 @@ class Simulation:
         N.check(N.lib().pg_get_pair_log(self.h, int(n), N.ptr(c, C.c_uint64), N.ptr(hs, C.c_uint64)))
         return c, hs
 
+    def postprocess(self, node_damage=False):
+        """On-device post-processing of the current state (pg_postprocess): grain means of vel,
+        acc and CurrPos, grain force sums, grain and (optionally) node damage, per-instance
+        sum of vol*rho*acc and volume fraction."""
+        G, I, D, Nn = self.setup.n_grains, self.setup.n_instances, self.dim, self.setup.n_nodes
+        out = dict(grain_mean_vel=np.empty((G, D)), grain_mean_acc=np.empty((G, D)),
+                   grain_mean_currpos=np.empty((G, D)), grain_force=np.empty((G, D)),
+                   grain_damage=np.empty(G), inertial_force=np.empty((I, D)), volume_fraction=np.empty(I))
+        if node_damage:
+            out["node_damage"] = np.empty(Nn)
+        p = N.Post()
+        for k, v in out.items():
+            setattr(p, k, N.ptr(v, C.c_double))
+        N.check(N.lib().pg_postprocess(self.h, C.byref(p)))
+        return out
+
     def device_status(self):
         st = C.c_int32()
         tc = C.c_uint64()
