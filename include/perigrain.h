@@ -118,6 +118,10 @@ typedef struct pg_config {
   uint32_t block_size;     /* threads per block of the fused force kernel (0: default 128) */
   int32_t autotune;        /* 1: pick block_size and cells_per_node by timing trial runs */
   uint32_t cells_per_node; /* contact-grid capacity per node (0: 4 in 2D, 8 in 3D) */
+  int32_t timeloop;        /* 0: run_timeloop (timeloop.h:501-1015); 1: run_timeloop_worm
+                              (timeloop.h:1018-1369): gait clamps of local nodes 0-3, external
+                              force in the first of three 1000-step phases only, contact and walls
+                              for every movable grain (no stoppable gate), no torque or ramp */
 } pg_config;
 
 /* ---- lifecycle ---------------------------------------------------------------------------- */

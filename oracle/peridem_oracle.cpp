@@ -336,7 +336,7 @@ struct orc_sim {
       Grain c1 = g, c2 = g;
       visit(c1, c2, true);
     }
-    if (g.stoppable) {
+    if (g.stoppable || cfg.timeloop == 1) {
       std::vector<double> C = minmax(g);
       for (uint32_t gj = in.g0; gj < in.g1; ++gj) {
         if (gj == gi) continue;
@@ -351,6 +351,7 @@ struct orc_sim {
 
   void force_instance(Inst& in, const std::vector<std::vector<double>>& boxes, uint64_t* pcp, uint64_t* php) {
     uint64_t pc = 0, ph = 0;
+    const bool worm = cfg.timeloop == 1;
     {
       // cell grid of this instance
       const double cell = in.Rc > 0 ? in.Rc * 1.01 : 1.0;
@@ -402,14 +403,14 @@ struct orc_sim {
               uint32_t gj = std::get<1>(cd), j = std::get<2>(cd);
               if (gj == gi) {
                 if (self && cfg.self_contact) pair(g, i, g, j, true, in, fi, &pc, &ph);
-              } else if (g.stoppable && intersects(boxes[gi], boxes[gj], in.Rc)) {
+              } else if ((g.stoppable || worm) && intersects(boxes[gi], boxes[gj], in.Rc)) {
                 pair(g, i, G[gj], j, false, in, fi, &pc, &ph);
               }
             }
             for (uint32_t c = 0; c < D; ++c) ft[i * D + c] = fi[c];
           }
           // walls
-          if (g.stoppable && in.allow_wall && !within_interior(boxes[gi], in.wall, in.Rc)) {
+          if ((g.stoppable || worm) && in.allow_wall && !within_interior(boxes[gi], in.wall, in.Rc)) {
             std::vector<uint32_t> order;
             if (cfg.nl_bdry_only) {
               order = g.bdry;
@@ -435,8 +436,12 @@ struct orc_sim {
               }
             }
           }
-          // external force
-          if (cfg.gradient_extforce) {
+          // external force; run_timeloop_worm: ft_i += ((t_num + 1) % 2) * extforce, no ramp and
+          // no torque (timeloop.h:1171)
+          if (worm) {
+            const double gate = (double)((worm_phase(t) + 1) % 2);
+            for (size_t k = 0; k < ft.size(); ++k) ft[k] += gate * g.extf[k];
+          } else if (cfg.gradient_extforce) {
             double sc = (double)t / (double)cfg.extforce_maxstep;
             if (sc > 1) sc = 1;
             for (size_t k = 0; k < ft.size(); ++k) ft[k] += sc * g.extf[k];
@@ -444,7 +449,7 @@ struct orc_sim {
             for (size_t k = 0; k < ft.size(); ++k) ft[k] += g.extf[k];
           }
           // torque about mean_CurrPos
-          if (cfg.enable_torque) {
+          if (cfg.enable_torque && !worm) {
             double m[3] = {0, 0, 0};
             for (uint32_t i = 0; i < g.n; ++i)
               for (uint32_t c = 0; c < D; ++c) m[c] += (g.pos[i * D + c] + g.disp[i * D + c]);
@@ -474,6 +479,8 @@ struct orc_sim {
     *php += ph;
   }
 
+  static uint32_t worm_phase(uint64_t t) { return ((t / 1000) % 3 == 0) ? 0u : 1u; }
+
   void step() {
     const double dt = cfg.dt;
     for (auto& in : I)
@@ -500,6 +507,7 @@ struct orc_sim {
     log_count.push_back(pc);
     log_hash.push_back(ph);
     // loop 3: velocity update
+    const bool worm = cfg.timeloop == 1;
     for (auto& g : G) {
       if (!g.movable) continue;
       double orho = 1 / g.rho;
@@ -517,6 +525,20 @@ struct orc_sim {
           g.vel[cid * D + c] = 0;
           g.acc[cid * D + c] = 0;
         }
+      if (worm) {
+        // gait clamps (timeloop.h:1213-1244): nodes 0, 3 or 1, 2 held, then no y motion for 0-3
+        const uint32_t ph = worm_phase(t);
+        const uint32_t held[2][2] = {{0, 3}, {1, 2}};
+        for (uint32_t cid : held[ph])
+          for (uint32_t c = 0; c < D; ++c) {
+            g.vel[cid * D + c] = 0;
+            g.acc[cid * D + c] = 0;
+          }
+        for (uint32_t cid = 0; cid < 4; ++cid) {
+          g.vel[cid * D + 1] = 0;
+          g.acc[cid * D + 1] = 0;
+        }
+      }
     }
     // wall move
     for (auto& in : I)

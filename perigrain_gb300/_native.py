@@ -43,7 +43,7 @@ class Config(C.Structure):
         ("enable_torque", C.c_int32), ("gradient_extforce", C.c_int32), ("extforce_maxstep", C.c_uint32),
         ("precision", C.c_int32), ("record_pairs", C.c_int32), ("pair_log_capacity", C.c_uint32),
         ("first_step", C.c_uint32), ("max_contacts", C.c_uint32), ("block_size", C.c_uint32),
-        ("autotune", C.c_int32), ("cells_per_node", C.c_uint32),
+        ("autotune", C.c_int32), ("cells_per_node", C.c_uint32), ("timeloop", C.c_int32),
     ]
 
 

@@ -86,6 +86,22 @@ __device__ __forceinline__ void record_masks(const Dev& P, uint32_t d, bool act,
   P.rec_wall[d] = wbits;
 }
 
+// Gait clamps of run_timeloop_worm (timeloop.h:1213-1244) on the node with grain-local index li:
+// vel = acc = 0 for nodes 0 and 3 (phase 0) or 1 and 2 (phase 1), then no y motion for nodes 0-3.
+template <int D, class TA, class TV>
+__device__ __forceinline__ void worm_clamp(uint32_t li, uint32_t phase, TA (&a)[D], TV (&v)[D]) {
+  if ((phase == 0 && (li == 0 || li == 3)) || (phase == 1 && (li == 1 || li == 2))) {
+    for (int c = 0; c < D; ++c) {
+      a[c] = 0;
+      v[c] = 0;
+    }
+  }
+  if (li < 4) {
+    a[1] = 0;
+    v[1] = 0;
+  }
+}
+
 // Tape of the step (REC with rec_x): the CurrPos and velocity node d's forces saw, and (first
 // threads) the wall positions and the step number.
 template <int D>

@@ -166,6 +166,7 @@ struct Dev {
   uint32_t extforce_maxstep;
   uint32_t max_cand;
   int32_t grain_contact;  // contact parameters from GrainDev (pair mean) instead of InstDev
+  int32_t worm;           // run_timeloop_worm semantics (pg_config::timeloop == 1)
   // mask recording (force kernels instantiated with REC = true): per node of this step the
   // offset and count of its active contact entries in rec_ent (entry = partner | friction
   // branch << 30, FR_*) and the wall bits (4 per wall side in call order: in contact, friction
@@ -223,6 +224,10 @@ __host__ __device__ inline double ordered_to_dbl(unsigned long long k) {
 #endif
   return x;
 }
+
+// Gait phase of run_timeloop_worm at step t (timeloop.h:1097-1107): 0 in the first of every three
+// 1000-step periods (front nodes 0 and 3 held, external force on), 1 otherwise (back nodes 1, 2).
+__host__ __device__ inline uint32_t worm_phase(uint32_t t) { return ((t / 1000u) % 3u == 0u) ? 0u : 1u; }
 
 __host__ __device__ inline uint64_t splitmix64(uint64_t x) {
   x += 0x9e3779b97f4a7c15ull;

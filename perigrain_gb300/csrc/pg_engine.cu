@@ -325,6 +325,8 @@ static int create_impl(const pg_setup_desc* s, const pg_config* cfg_in, pg_handl
   P.record_pairs = cfg.record_pairs;
   P.extforce_maxstep = cfg.extforce_maxstep;
   P.max_cand = cfg.max_contacts;
+  if (cfg.timeloop != 0 && cfg.timeloop != 1) return fail(PG_EINVAL, "timeloop must be 0 or 1");
+  P.worm = cfg.timeloop;
 
   h->grain_node_offset.assign(s->grain_node_offset, s->grain_node_offset + G + 1);
   h->bond_offset.assign(s->bond_offset, s->bond_offset + N + 1);

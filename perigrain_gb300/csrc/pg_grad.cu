@@ -148,6 +148,7 @@ static void enqueue_replay_step(pg_handle* h, int parity, const pg_masks* m, uin
 
 static int check_grad_ok(pg_handle* h) {
   if (h->P.enable_torque) return fail(PG_EINVAL, "torque is not differentiated (enable_torque must be 0)");
+  if (h->P.worm) return fail(PG_EINVAL, "the worm time loop is not differentiated");
   std::vector<GrainDev> g(h->P.G);
   CU(cudaMemcpy(g.data(), h->P.grain, g.size() * sizeof(GrainDev), cudaMemcpyDeviceToHost));
   for (uint32_t k = 0; k < h->P.G; ++k)

@@ -581,7 +581,7 @@ static int write_tc(pg_handle* h, pg_setup* s, const std::string& dir, uint32_t 
                     const std::vector<double>& cur, const std::vector<double>& vel,
                     const std::vector<double>& acc, const std::vector<double>& force,
                     const std::vector<uint8_t>& alive, const std::vector<double>& wall,
-                    const std::vector<double>& reaction) {
+                    const std::vector<double>& reaction, bool connectivity = true) {
   (void)h;
   const uint32_t D = s->dim;
   char buf[64];
@@ -597,9 +597,11 @@ static int write_tc(pg_handle* h, pg_setup* s, const std::string& dir, uint32_t 
     w.add_dataset(pre + "vel", h5l::DType::F64, {n, D}, vel.data() + (size_t)n0 * D);
     w.add_dataset(pre + "acc", h5l::DType::F64, {n, D}, acc.data() + (size_t)n0 * D);
     w.add_dataset(pre + "force", h5l::DType::F64, {n, D}, force.data() + (size_t)n0 * D);
-    std::vector<uint32_t> conn;
-    rows_to_conn(s, g, alive.data(), &conn);
-    w.add_dataset(pre + "Connectivity", h5l::DType::U32, {conn.size() / 2, 2}, conn.data());
+    if (connectivity) {  // run_timeloop_worm writes none (timeloop.h:1283-1292)
+      std::vector<uint32_t> conn;
+      rows_to_conn(s, g, alive.data(), &conn);
+      w.add_dataset(pre + "Connectivity", h5l::DType::U32, {conn.size() / 2, 2}, conn.data());
+    }
   }
   if (!w.write(dir + "/tc_" + buf + ".h5")) return iofail(PG_EIO, "cannot write " + dir + "/tc_" + buf + ".h5");
   h5l::Writer ww;
@@ -609,8 +611,7 @@ static int write_tc(pg_handle* h, pg_setup* s, const std::string& dir, uint32_t 
   return PG_OK;
 }
 
-extern "C" int pg_write_snapshot(pg_handle* h, pg_setup* s, const char* out_dir, uint32_t counter) {
-  if (!h || !s || !out_dir) return iofail(PG_EINVAL, "null argument");
+static int snapshot(pg_handle* h, pg_setup* s, const char* out_dir, uint32_t counter, bool connectivity) {
   const uint32_t D = s->dim;
   std::vector<double> cur((size_t)s->N * D), vel(cur.size()), acc(cur.size()), force(cur.size());
   std::vector<uint8_t> alive(s->bond_local.size() + 1);
@@ -621,7 +622,12 @@ extern "C" int pg_write_snapshot(pg_handle* h, pg_setup* s, const char* out_dir,
       (rc = pg_get_bond_alive(h, alive.data())) || (rc = pg_get_wall(h, wall.data())) ||
       (rc = pg_get_reaction(h, reaction.data())))
     return iofail(rc, pg_last_error());
-  return write_tc(h, s, out_dir, counter, cur, vel, acc, force, alive, wall, reaction);
+  return write_tc(h, s, out_dir, counter, cur, vel, acc, force, alive, wall, reaction, connectivity);
+}
+
+extern "C" int pg_write_snapshot(pg_handle* h, pg_setup* s, const char* out_dir, uint32_t counter) {
+  if (!h || !s || !out_dir) return iofail(PG_EINVAL, "null argument");
+  return snapshot(h, s, out_dir, counter, true);
 }
 
 // =============================================================================================
@@ -739,6 +745,11 @@ extern "C" int pg_run_simulation(const char* root_c, uint32_t dim, int32_t preci
   cfg.extforce_maxstep = C.extforce_maxstep;
   cfg.precision = precision;
   cfg.first_step = 1;
+  // PERIGRAIN_TIMELOOP=worm: the reference's run_timeloop_worm (timeloop.h:1018-1369) instead of
+  // run_timeloop -- no hooks, no Connectivity in tc_ files, its progress line
+  const char* tl_env = std::getenv("PERIGRAIN_TIMELOOP");
+  const bool worm = tl_env && std::string(tl_env) == "worm";
+  cfg.timeloop = worm ? 1 : 0;
   pg_handle* H = nullptr;
   rc = pg_create(&desc, &cfg, &H);
   if (rc) return iofail(rc, std::string("pg_create: ") + pg_last_error());
@@ -766,16 +777,16 @@ extern "C" int pg_run_simulation(const char* root_c, uint32_t dim, int32_t preci
   uint64_t too_close_seen = 0;
   uint32_t t = 1;
   while (t <= T) {
-    // hooks at the start of step t (timeloop.h:612-650)
-    if (C.set_movable_index != -1 && (uint32_t)C.set_movable_timestep == t) {
+    // hooks at the start of step t (timeloop.h:612-650); the worm loop has none
+    if (!worm && C.set_movable_index != -1 && (uint32_t)C.set_movable_timestep == t) {
       std::cout << "Setting particle " << C.set_movable_index << " to movable on timestep " << t << std::endl;
       if ((rc = pg_set_grain_flags(H, (uint32_t)C.set_movable_index, 1, -1))) return iofail(rc, pg_last_error());
     }
-    if (C.set_stoppable_index != -1 && (uint32_t)C.set_stoppable_timestep == t) {
+    if (!worm && C.set_stoppable_index != -1 && (uint32_t)C.set_stoppable_timestep == t) {
       std::cout << "Setting particle " << C.set_stoppable_index << " to stoppable on timestep " << t << std::endl;
       if ((rc = pg_set_grain_flags(H, (uint32_t)C.set_stoppable_index, -1, 1))) return iofail(rc, pg_last_error());
     }
-    if (C.reset_partzero_y && C.reset_partzero_y_timestep == t && S->G > 1) {
+    if (!worm && C.reset_partzero_y && C.reset_partzero_y_timestep == t && S->G > 1) {
       std::vector<double> pos((size_t)S->N * dim), disp(pos.size());
       if ((rc = pg_get_field(H, PG_FIELD_POS, pos.data())) || (rc = pg_get_field(H, PG_FIELD_DISP, disp.data())))
         return iofail(rc, pg_last_error());
@@ -801,9 +812,9 @@ extern "C" int pg_run_simulation(const char* root_c, uint32_t dim, int32_t preci
     auto hook = [&](int64_t ts) {
       if (ts > (int64_t)t && ts - 1 < (int64_t)e) e = (uint32_t)(ts - 1);
     };
-    if (C.set_movable_index != -1) hook((uint32_t)C.set_movable_timestep);
-    if (C.set_stoppable_index != -1) hook((uint32_t)C.set_stoppable_timestep);
-    if (C.reset_partzero_y) hook(C.reset_partzero_y_timestep);
+    if (!worm && C.set_movable_index != -1) hook((uint32_t)C.set_movable_timestep);
+    if (!worm && C.set_stoppable_index != -1) hook((uint32_t)C.set_stoppable_timestep);
+    if (!worm && C.reset_partzero_y) hook(C.reset_partzero_y_timestep);
     if (e < t) e = t;
     if ((rc = pg_step(H, e - t + 1))) return iofail(rc, pg_last_error());
     t = e + 1;
@@ -812,7 +823,7 @@ extern "C" int pg_run_simulation(const char* root_c, uint32_t dim, int32_t preci
       uint64_t tc = 0;
       pg_get_device_status(H, nullptr, &tc);
       for (; too_close_seen < tc; ++too_close_seen) std::cout << "Error: nodes too close" << std::endl;
-      if ((rc = pg_write_snapshot(H, S, out.c_str(), counter))) return rc;
+      if ((rc = snapshot(H, S, out.c_str(), counter, !worm))) return rc;
       if (tsd) {
         const uint32_t G = S->G;
         std::vector<double> v((size_t)G * dim), a(v.size()), x(v.size()), f(v.size()), dmg(G), fs(dim), phi(1),
@@ -848,6 +859,17 @@ extern "C" int pg_run_simulation(const char* root_c, uint32_t dim, int32_t preci
         avg_duration /= avgsteps;
       }
       int rem_counts = (int)last_counter - (int)counter;
+      if (worm) {
+        // the worm loop's line (timeloop.h:1331-1350): t, counter, duration/100, remaining m s, ctime
+        avg_duration = 0;
+        if (run_time.size() >= 10)
+          for (size_t cc = run_time.size() - avgsteps; cc < run_time.size(); ++cc) avg_duration += run_time[cc];
+        avg_duration /= avgsteps;
+        const double rem_min = (rem_counts * avg_duration) / 1e3 / 60;
+        time_t now = time(NULL);
+        std::cout << e << "\t" << counter << "\t" << duration.count() / 100 << "\t" << (int)rem_min << "m"
+                  << (rem_min - (int)rem_min) * 60 << "s" << "\t" << ctime(&now);
+      } else {
       int rem_s = (int)((rem_counts * avg_duration) / 1e3);
       char rem[32];
       std::snprintf(rem, sizeof rem, "%02d:%02d:%02d", (rem_s / 60) / 60, (rem_s / 60) % 60, rem_s % 60);
@@ -857,6 +879,7 @@ extern "C" int pg_run_simulation(const char* root_c, uint32_t dim, int32_t preci
       std::cout << std::left << std::setw(column_w) << e << std::left << std::setw(column_w) << counter
                 << std::left << std::setw(column_w) << (double)duration.count() / 1000 << std::left
                 << std::setw(column_w + 5) << rem << std::left << std::setw(column_w + 10) << ts << std::endl;
+      }
       run_time.push_back((double)duration.count());
       t_ind.push_back(e);
       ++counter;

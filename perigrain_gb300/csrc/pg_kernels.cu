@@ -174,7 +174,9 @@ __global__ void __launch_bounds__(128) k_force(const Dev P) {
   const InstDev& in = P.inst[gr.inst];
   const bool p_bdry = !P.nl_bdry_only || (act && P.bdry_rank[d] != NONE);
   const bool selfc = mov && P.enable_fracture && (gr.flags & GF_BREAKABLE) && P.self_contact;
-  const bool other = mov && (gr.flags & GF_STOPPABLE);
+  // contact with other grains and walls only for stoppable grains (timeloop.h:719), for every
+  // movable grain in the worm loop (timeloop.h:1146-1168)
+  const bool other = mov && (P.worm || (gr.flags & GF_STOPPABLE));
   double xpc[D];
   if (act) ldv<D>(P.cur, d, xpc);
 
@@ -416,7 +418,13 @@ __global__ void __launch_bounds__(128) k_force(const Dev P) {
   }
 
   // ---- external force and torque (timeloop.h:774-824) ----
-  if (mov) {
+  if (mov && P.worm) {
+    // ft_i += ((t_num + 1) % 2) * extforce (timeloop.h:1171)
+    double ef[D];
+    ldv<D>(P.extf, d, ef);
+    const double gate = (double)((worm_phase(t) + 1u) % 2u);
+    for (int c = 0; c < D; ++c) f[c] = f[c] + gate * ef[c];
+  } else if (mov) {
     double ef[D];
     ldv<D>(P.extf, d, ef);
     if (P.gradient_extforce) {
@@ -465,6 +473,7 @@ __global__ void __launch_bounds__(128) k_force(const Dev P) {
         }
         P.clamp_pending[d] = 1;
       }
+      if (P.worm) worm_clamp<D>(d - gr.node_begin, worm_phase(t), a, v);
       stv<D>(P.acc, d, a);
       stv<D>(P.vel_out, d, v);
     } else {

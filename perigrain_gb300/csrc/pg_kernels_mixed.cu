@@ -371,7 +371,7 @@ __global__ void __launch_bounds__(128) k_force_mx(const Dev P) {
   const InstDev& in = P.inst[gr.inst];
   const bool p_bdry = !P.nl_bdry_only || (act && P.bdry_rank[d] != NONE);
   const bool selfc = mov && P.enable_fracture && (gr.flags & GF_BREAKABLE) && P.self_contact;
-  const bool other = mov && (gr.flags & GF_STOPPABLE);
+  const bool other = mov && (P.worm || (gr.flags & GF_STOPPABLE));
   float vp[D];
   for (int c = 0; c < D; ++c) vp[c] = act ? (float)vpd[c] : 0.f;
 
@@ -605,7 +605,12 @@ __global__ void __launch_bounds__(128) k_force_mx(const Dev P) {
     }
   }
 
-  if (mov) {
+  if (mov && P.worm) {
+    float ef[D];
+    ldvf<D>(P.extf_f, d, ef);
+    const float gate = (float)((worm_phase(t) + 1u) % 2u);
+    for (int c = 0; c < D; ++c) f[c] = fmaf(gate, ef[c], f[c]);
+  } else if (mov) {
     float ef[D];
     ldvf<D>(P.extf_f, d, ef);
     float sc = 1.f;
@@ -650,6 +655,7 @@ __global__ void __launch_bounds__(128) k_force_mx(const Dev P) {
         }
         P.clamp_pending[d] = 1;
       }
+      if (P.worm) worm_clamp<D>(d - gr.node_begin, worm_phase(t), a, v);
       stvf<D>(P.acc_f, d, a);
       stv<D>(P.vel_out, d, v);
     } else {

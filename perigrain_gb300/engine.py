@@ -18,7 +18,7 @@ class Simulation:
     def __init__(self, setup, dt, enable_fracture=1, nl_bdry_only=0, allow_damping=1, allow_friction=1,
                  self_contact=1, enable_torque=0, gradient_extforce=0, extforce_maxstep=0, precision="fp64",
                  record_pairs=False, pair_log_capacity=1024, first_step=1, max_contacts=48, block_size=0,
-                 autotune=False, cells_per_node=0):
+                 autotune=False, cells_per_node=0, timeloop=0):
         L = N.lib()
         self.setup = setup
         self.dim = setup.dim
@@ -41,6 +41,7 @@ class Simulation:
         cfg.block_size = int(block_size)
         cfg.autotune = int(bool(autotune))
         cfg.cells_per_node = int(cells_per_node)
+        cfg.timeloop = 1 if timeloop in (1, "worm") else 0
         self.cfg = cfg
         self._desc = setup.desc()
         h = C.c_void_p()

@@ -12,7 +12,8 @@ from perigrain_gb300 import h5
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 ORACLE = os.path.join(ROOT, "oracle")
 LIBORACLE = os.path.join(ORACLE, "liboracle.so")
-REF_BIN = {2: os.path.join(ORACLE, "_ref", "simulate2d"), 3: os.path.join(ORACLE, "_ref", "simulate3d")}
+REF_BIN = {2: os.path.join(ORACLE, "_ref", "simulate2d"), 3: os.path.join(ORACLE, "_ref", "simulate3d"),
+           "worm": os.path.join(ORACLE, "_ref", "simulate2d_worm")}
 
 _lib = None
 
@@ -51,7 +52,8 @@ class OracleSim:
     """Same interface as perigrain_gb300.Simulation, computed by the CPU oracle."""
 
     def __init__(self, setup, dt, enable_fracture=1, nl_bdry_only=0, allow_damping=1, allow_friction=1,
-                 self_contact=1, enable_torque=0, gradient_extforce=0, extforce_maxstep=0, first_step=1, **_):
+                 self_contact=1, enable_torque=0, gradient_extforce=0, extforce_maxstep=0, first_step=1, timeloop=0,
+                 **_):
         L = oracle_lib()
         self.setup = setup
         self.dim = setup.dim
@@ -66,6 +68,7 @@ class OracleSim:
         cfg.gradient_extforce = int(gradient_extforce)
         cfg.extforce_maxstep = int(extforce_maxstep)
         cfg.first_step = int(first_step)
+        cfg.timeloop = 1 if timeloop in (1, "worm") else 0
         self._desc = setup.desc()
         h = C.c_void_p()
         assert L.orc_create(C.byref(self._desc), C.byref(cfg), C.byref(h)) == 0
@@ -156,9 +159,10 @@ def make_case_dir(tmp, setup, conf):
     return tmp
 
 
-def run_reference(case_dir, dim, timeout=600):
-    """Run the reference simulator (compiled unmodified against the shims) in case_dir."""
-    exe = REF_BIN[dim]
+def run_reference(case_dir, dim, timeout=600, timeloop=None):
+    """Run the reference simulator (compiled unmodified against the shims) in case_dir;
+    timeloop="worm" runs the reference's run_timeloop_worm (2D)."""
+    exe = REF_BIN["worm" if timeloop == "worm" else dim]
     if not os.path.exists(exe):
         build_oracle()
     if not os.path.exists(exe):
@@ -170,12 +174,14 @@ def run_reference(case_dir, dim, timeout=600):
     return r.stdout
 
 
-def read_tc(case_dir, counter, n_grains, dim):
+def read_tc(case_dir, counter, n_grains, dim, connectivity=True):
     fn = os.path.join(case_dir, "output", "hdf5", "tc_%05d.h5" % counter)
     out = {}
     for key in ("CurrPos", "vel", "acc", "force"):
         out[key] = np.concatenate([h5.read(fn, "P_%05d/%s" % (g, key), np.float64) for g in range(n_grains)])
-    out["Connectivity"] = [h5.read(fn, "P_%05d/Connectivity" % g, np.uint32).reshape(-1, 2) for g in range(n_grains)]
+    if connectivity:
+        out["Connectivity"] = [h5.read(fn, "P_%05d/Connectivity" % g, np.uint32).reshape(-1, 2)
+                               for g in range(n_grains)]
     fw = os.path.join(case_dir, "output", "hdf5", "wall_%05d.h5" % counter)
     out["wall_info"] = h5.read(fw, "wall_info", np.float64).ravel()
     out["reaction"] = h5.read(fw, "reaction", np.float64)

@@ -39,6 +39,10 @@ CASES = {
                               set_stoppable_index=0, set_stoppable_timestep=80, allow_damping=0)),
     "nofracture2d": dict(setup=dict(dim=2, speed=60.0), conf=dict(timesteps=200, modulo=100, enable_fracture=0,
                                                                   allow_friction=0)),
+    # run_timeloop_worm (timeloop.h:1018-1369): both gait phases (t < 1000 and t >= 1000), external
+    # force gated by the phase, and a grain that is not stoppable still in contact
+    "worm2d": dict(setup=dict(dim=2, speed=30.0, extforce=True), stoppable={1: 0}, timeloop="worm",
+                   conf=dict(timesteps=1200, modulo=200)),
 }
 
 
@@ -49,6 +53,14 @@ def case_setup(spec):
     for g, v in spec.get("stoppable", {}).items():
         s.stoppable[g] = v
     return s
+
+
+def case_kwargs(spec, conf):
+    """Engine / oracle keyword arguments of a case (the time-loop variant is not a config key)."""
+    kw = O.engine_kwargs(conf)
+    if spec.get("timeloop") == "worm":
+        kw["timeloop"] = 1
+    return kw
 
 
 def case_conf(spec, s):
@@ -64,26 +76,29 @@ def setup_digest(s):
     return h.hexdigest()
 
 
-def main():
+def main(names=None):
     O.build_oracle()
     for name, spec in CASES.items():
+        if names and name not in names:
+            continue
         s = case_setup(spec)
         conf = case_conf(spec, s)
         d = tempfile.mkdtemp(prefix="golden_")
         O.make_case_dir(d, s, conf)
-        O.run_reference(d, s.dim)
+        O.run_reference(d, s.dim, timeloop=spec.get("timeloop"))
         out = {"meta": np.frombuffer(json.dumps(dict(conf=conf, spec=spec, digest=setup_digest(s))).encode(),
                                      np.uint8)}
         nsnap = conf["timesteps"] // conf["modulo"]
+        worm = spec.get("timeloop") == "worm"  # the worm loop writes no Connectivity
         for k in range(1, nsnap + 1):
-            tc = O.read_tc(d, k, s.n_grains, s.dim)
+            tc = O.read_tc(d, k, s.n_grains, s.dim, connectivity=not worm)
             for f in ("CurrPos", "vel", "acc", "force", "wall_info", "reaction"):
                 out["%d/%s" % (k, f)] = tc[f]
-            for g, c in enumerate(tc["Connectivity"]):
+            for g, c in enumerate(tc.get("Connectivity", [])):
                 out["%d/conn%d" % (k, g)] = c
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
         print(name, s.n_nodes, "nodes", nsnap, "snapshots")
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

@@ -11,7 +11,7 @@ import numpy as np
 import pytest
 
 import _oracle as O
-from golden.make_golden import CASES, case_setup
+from golden.make_golden import CASES, case_kwargs, case_setup
 from perigrain_gb300 import Simulation, h5
 
 pytestmark = pytest.mark.gpu
@@ -34,7 +34,7 @@ def _check_state(name, k, z, fields, reaction, wall, conn):
     else:
         assert np.abs(reaction - zr).max() <= 1e-7 * max(np.abs(zr).max(), 1e-30)
     assert np.array_equal(wall, z["%d/wall_info" % k])
-    for g, c in enumerate(conn):
+    for g, c in enumerate(conn or []):
         assert np.array_equal(c, z["%d/conn%d" % (k, g)]), (name, k, g)
 
 
@@ -43,11 +43,13 @@ def test_engine_matches_reference_outputs(name):
     z, meta = O.load_golden(name)
     s = case_setup(CASES[name])
     conf = meta["conf"]
-    sim = Simulation(s, **O.engine_kwargs(conf))
+    sim = Simulation(s, **case_kwargs(CASES[name], conf))
+    worm = CASES[name].get("timeloop") == "worm"
 
     def check(k):
         fields = {f: sim.field(f) for f in ("CurrPos", "vel", "acc", "force")}
-        _check_state(name, k, z, fields, sim.reaction()[0], sim.wall()[0], O.conn_from_alive(s, sim.bond_alive()))
+        conn = None if worm else O.conn_from_alive(s, sim.bond_alive())
+        _check_state(name, k, z, fields, sim.reaction()[0], sim.wall()[0], conn)
 
     O.drive(sim, conf, s.n_grains, check)
 
@@ -60,7 +62,9 @@ def test_dropin_executable_matches_reference_files(name):
     d = tempfile.mkdtemp(prefix="dropin_")
     O.make_case_dir(d, s, conf)
     exe = os.path.join(BIN, "simulate%dd" % s.dim)
-    r = subprocess.run([exe], cwd=d, capture_output=True, text=True, timeout=300)
+    worm = CASES[name].get("timeloop") == "worm"
+    env = dict(os.environ, PERIGRAIN_TIMELOOP="worm") if worm else None
+    r = subprocess.run([exe], cwd=d, capture_output=True, text=True, timeout=300, env=env)
     assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
     assert "Runtime:" in r.stdout
     out = os.path.join(d, "output", "hdf5")
@@ -68,9 +72,9 @@ def test_dropin_executable_matches_reference_files(name):
     assert flc.tolist() == [1, conf["timesteps"] // conf["modulo"]]
     assert h5.read(os.path.join(out, "plotinfo.h5"), "dimension", np.uint32).ravel()[0] == s.dim
     for k in range(1, conf["timesteps"] // conf["modulo"] + 1):
-        tc = O.read_tc(d, k, s.n_grains, s.dim)
+        tc = O.read_tc(d, k, s.n_grains, s.dim, connectivity=not worm)
         fields = {f: tc[f] for f in ("CurrPos", "vel", "acc", "force")}
-        _check_state(name, k, z, fields, tc["reaction"], tc["wall_info"], tc["Connectivity"])
+        _check_state(name, k, z, fields, tc["reaction"], tc["wall_info"], tc.get("Connectivity"))
     rt = h5.read(os.path.join(out, "run_time.h5"), "t_ind", np.float64).ravel()
     assert rt.tolist() == [float(conf["modulo"] * (k + 1)) for k in range(len(rt))]
 
