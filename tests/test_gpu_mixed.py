@@ -124,3 +124,17 @@ def test_mixed_settling_with_gravity_and_walls():
     g.step(300)
     r.step(300)
     assert _pos_err(g, r) <= POS_RTOL
+
+
+def test_mixed_block_size_does_not_change_results():
+    """Per-node arithmetic does not depend on the launch shape: block sizes 64 and 128 (different
+    shared-memory neighbour windows in 2D, different grids) give identical runs."""
+    s = setups.concat([setups.small_pair(dim=2, seed=51 + k, wall=True, speed=35.0) for k in range(3)])
+    runs = []
+    for b in (64, 128):
+        g = Simulation(s, dt=2e-8, enable_fracture=1, precision="mixed", block_size=b)
+        g.step(300)
+        runs.append(g)
+    for f in ("CurrPos", "vel", "acc", "force"):
+        assert np.array_equal(runs[0].field(f), runs[1].field(f)), f
+    assert np.array_equal(runs[0].bond_alive(), runs[1].bond_alive())
