@@ -317,7 +317,7 @@ def main():
     setup, spec = build_workload(a.workload, rank)
     kw = engine_kwargs(spec, a.precision)
     sim = Simulation(setup, autotune=not a.profile_run, **kw)
-    tuned = sim.launch_config()
+    tuned = dict(sim.launch_config(), contact_skin=sim.contact_skin())
     sim.step(a.warmup)
     sim.synchronize()
     if a.profile_run:

@@ -116,8 +116,13 @@ typedef struct pg_config {
   uint32_t first_step;     /* t of the first step taken (1, or resume_ind*modulo + 1) */
   uint32_t max_contacts;   /* per-node contact candidate capacity (default 48 when 0) */
   uint32_t block_size;     /* threads per block of the fused force kernel (0: default 128) */
-  int32_t autotune;        /* 1: pick block_size and cells_per_node by timing trial runs */
+  int32_t autotune;        /* 1: pick block_size, cells_per_node and contact_skin by timing trial runs */
   uint32_t cells_per_node; /* contact-grid capacity per node (0: 4 in 2D, 8 in 3D) */
+  double contact_skin;     /* > 0: keep per-node contact candidate lists built with radius
+                              R_c (1 + contact_skin), rebuilt when a node has moved more than
+                              0.45 contact_skin R_c since the last build (results are unchanged);
+                              0: search the contact grid every step. Default 0.25; autotune
+                              also picks it */
   int32_t timeloop;        /* 0: run_timeloop (timeloop.h:501-1015); 1: run_timeloop_worm
                               (timeloop.h:1018-1369): gait clamps of local nodes 0-3, external
                               force in the first of three 1000-step phases only, contact and walls
@@ -186,6 +191,8 @@ int pg_get_pair_log(pg_handle* h, uint32_t n, uint64_t* count, uint64_t* hash);
 int pg_get_device_status(pg_handle* h, int32_t* status, uint64_t* too_close_events);
 /* Launch configuration in use (after autotuning): force-kernel block size, grid cells per node. */
 int pg_get_launch_config(pg_handle* h, uint32_t* block_size, uint32_t* cells_per_node);
+/* Contact candidate-list skin in use (fraction of R_c; 0: grid search every step). */
+int pg_get_contact_skin(pg_handle* h, double* skin);
 /* Number of kernel launches issued by the last pg_step call. */
 int pg_get_launch_count(pg_handle* h, uint64_t* launches);
 /* Per-kernel device time of the last pg_step call (CUDA events; needs timing enabled). */

@@ -43,7 +43,8 @@ class Config(C.Structure):
         ("enable_torque", C.c_int32), ("gradient_extforce", C.c_int32), ("extforce_maxstep", C.c_uint32),
         ("precision", C.c_int32), ("record_pairs", C.c_int32), ("pair_log_capacity", C.c_uint32),
         ("first_step", C.c_uint32), ("max_contacts", C.c_uint32), ("block_size", C.c_uint32),
-        ("autotune", C.c_int32), ("cells_per_node", C.c_uint32), ("timeloop", C.c_int32),
+        ("autotune", C.c_int32), ("cells_per_node", C.c_uint32), ("contact_skin", C.c_double),
+        ("timeloop", C.c_int32),
     ]
 
 
@@ -104,6 +105,7 @@ PROTOTYPES = [
     ("pg_get_device_status", C.c_int, [C.c_void_p, i32p, u64p]),
     ("pg_get_launch_count", C.c_int, [C.c_void_p, u64p]),
     ("pg_get_launch_config", C.c_int, [C.c_void_p, u32p, u32p]),
+    ("pg_get_contact_skin", C.c_int, [C.c_void_p, f64p]),
     ("pg_set_timing", C.c_int, [C.c_void_p, C.c_int32]),
     ("pg_get_kernel_times", C.c_int, [C.c_void_p, f64p, f64p, u64p]),
     ("pg_build_bonds", C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_double, C.c_void_p, C.c_uint64, u64p,

@@ -147,9 +147,14 @@ __device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* warp_s
   return base + x - v;
 }
 
+// With candidate lists the grid is rebuilt only on rebuild steps; the grid kernels return at once
+// on the other steps.
+__device__ __forceinline__ bool grid_idle(const Dev& P) { return P.cand_q && !*P.rebuild; }
+
 static __global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(const Dev P) {
   __shared__ uint32_t ws[32];
   __shared__ bool last;
+  if (grid_idle(P)) return;
   const uint32_t tile = blockIdx.x;
   const uint32_t base = tile * SCAN_TILE + threadIdx.x * SCAN_PER;
   uint32_t s = 0;
@@ -193,6 +198,7 @@ static __global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(const Dev P
 
 static __global__ void __launch_bounds__(SCAN_THREADS) k_scan_final(const Dev P) {
   __shared__ uint32_t ws[32];
+  if (grid_idle(P)) return;
   const uint32_t tile = blockIdx.x;
   const uint32_t base = tile * SCAN_TILE + threadIdx.x * SCAN_PER;
   uint32_t v[SCAN_PER];
@@ -239,6 +245,7 @@ static __global__ void __launch_bounds__(SCAN_THREADS) k_scan_final(const Dev P)
 }
 
 static __global__ void __launch_bounds__(256) k_scatter(const Dev P) {
+  if (grid_idle(P)) return;
   const uint32_t d = blockIdx.x * blockDim.x + threadIdx.x;
   if (d < P.N) P.sorted[P.cell_start[P.cell_key[d]] + P.cell_rank[d]] = d;
 }
@@ -422,6 +429,7 @@ static __global__ void __launch_bounds__(FINAL_THREADS) k_finalize(const Dev P) 
     }
     *P.wrec_count = 0;
     *P.step = t + 1;
+    if (P.cand_q) *P.rebuild = 0;
   }
   for (uint32_t p = tid; p < P.I * NS; p += blockDim.x) {
     InstDev* in = &P.inst[p / NS];
@@ -460,13 +468,122 @@ static __global__ void __launch_bounds__(FINAL_THREADS) k_finalize(const Dev P) 
 
 inline uint32_t cdiv(uint32_t a, uint32_t b) { return (a + b - 1) / b; }
 
-// Grid build shared by both precisions: exclusive scan of the bucket counts, then scatter.
+// ---------------------------------------------------------------------------------------------
+// Contact candidate lists (Verlet lists with a skin): on rebuild steps the grid is recounted and
+// every node's list rebuilt with radius R_c + skin; on the other steps the force kernels read the
+// lists instead of searching the grid. A pair within R_c at step t was within R_c + skin at the
+// last build while no node has moved more than skin/2 since (predict raises `rebuild` at 0.45 skin),
+// so every pair the grid search would evaluate is in the list, in the same order.
+// ---------------------------------------------------------------------------------------------
+// grid keys of a rebuild step (the grid-search path computes them in the predict kernels)
+template <int D>
+static __global__ void __launch_bounds__(256) k_keys(const Dev P) {
+  if (!*P.rebuild) return;
+  const uint32_t d = blockIdx.x * blockDim.x + threadIdx.x;
+  if (d >= P.N) return;
+  const InstDev& in = P.inst[P.grain[P.node_grain[d]].inst];
+  float rf[D];
+  ldf<D>(P.curf, d, rf);
+  int32_t ci[3] = {0, 0, 0};
+  for (int c = 0; c < D; ++c) ci[c] = cell_coord(rf[c], in.inv_cell_f, in.dims[c]);
+  const uint32_t key = in.table_off + ((uint32_t)ci[2] * in.dims[1] + (uint32_t)ci[1]) * in.dims[0] + (uint32_t)ci[0];
+  P.cell_key[d] = key;
+  P.cell_rank[d] = atomicAdd(&P.cell_count[key], 1u);
+}
+
+// Rebuild of node d's list: every node q of the 3x3 (3x3x3) cells within the FP32 radius pre_b that
+// the contact rules could pair with d (same grain: self-contact; other grain: stoppable, or any in
+// the worm loop; boundary nodes only when nl_bdry_only), sorted by the reference's visit order.
+// The bounding-box prefilter is applied per step, not here. Also records the displacement.
+template <int D>
+static __global__ void __launch_bounds__(128) k_cand_build(const Dev P) {
+  if (!*P.rebuild) return;
+  const uint32_t d = blockIdx.x * blockDim.x + threadIdx.x;
+  if (d >= P.N) return;
+  const uint32_t lane = d & 31, chunk = d >> 5;
+  constexpr uint32_t SF = (D == 2) ? 2 : 4;
+  double dp[D];
+  ldv<D>(P.disp, d, dp);
+  for (int c = 0; c < D; ++c) P.disp_b[(size_t)d * SF + c] = (float)dp[c];
+  const uint32_t g = P.node_grain[d];
+  const GrainDev gr = P.grain[g];
+  const bool mov = gr.flags & GF_MOVABLE;
+  const bool p_bdry = !P.nl_bdry_only || P.bdry_rank[d] != NONE;
+  const bool selfc = mov && P.enable_fracture && (gr.flags & GF_BREAKABLE) && P.self_contact;
+  const bool other = mov && (P.worm || (gr.flags & GF_STOPPABLE));
+  uint32_t n = 0;
+  if ((selfc || other) && p_bdry) {
+    const InstDev& in = P.inst[gr.inst];
+    float pf[D];
+    ldf<D>(P.curf, d, pf);
+    int32_t cc[3] = {0, 0, 0};
+    for (int c = 0; c < D; ++c) cc[c] = cell_coord(pf[c], in.inv_cell_f, in.dims[c]);
+    const float thr2 = in.pre_b * in.pre_b;
+    unsigned long long keys[CAND_CAP];
+    uint32_t idx[CAND_CAP];
+    const int z0 = (D == 3) ? max(cc[2] - 1, 0) : 0, z1 = (D == 3) ? min(cc[2] + 1, (int)in.dims[2] - 1) : 0;
+    const int y0 = max(cc[1] - 1, 0), y1 = min(cc[1] + 1, (int)in.dims[1] - 1);
+    const int x0 = max(cc[0] - 1, 0), x1 = min(cc[0] + 1, (int)in.dims[0] - 1);
+    for (int z = z0; z <= z1; ++z)
+      for (int y = y0; y <= y1; ++y) {
+        const uint32_t row = in.table_off + ((uint32_t)z * in.dims[1] + (uint32_t)y) * in.dims[0];
+        const uint32_t b0 = P.cell_start[row + x0], b1 = P.cell_start[row + x1 + 1];
+        for (uint32_t b = b0; b < b1; ++b) {
+          const uint32_t q = P.sorted[b];
+          if (q == d) continue;
+          float qf[D];
+          ldf<D>(P.curf, q, qf);
+          float d2 = 0.f;
+          for (int c = 0; c < D; ++c) {
+            const float dd = qf[c] - pf[c];
+            d2 += dd * dd;
+          }
+          if (d2 > thr2) continue;
+          const uint32_t gq = P.node_grain[q];
+          const bool same = gq == g;
+          if (same ? !selfc : !other) continue;
+          if (P.nl_bdry_only && P.bdry_rank[q] == NONE) continue;
+          const uint32_t sub = P.nl_bdry_only ? P.bdry_rank[q] : (q - P.grain[gq].node_begin);
+          const unsigned long long key =
+              ((unsigned long long)(same ? 0u : 1u) << 63) | ((unsigned long long)gq << 32) | sub;
+          if (n >= P.cand_cap) {
+            set_status(P.status, PG_ECAPACITY);
+            continue;
+          }
+          int k = (int)n++;
+          while (k > 0 && keys[k - 1] > key) {
+            keys[k] = keys[k - 1];
+            idx[k] = idx[k - 1];
+            --k;
+          }
+          keys[k] = key;
+          idx[k] = q;
+        }
+      }
+    const size_t base = (size_t)chunk * P.cand_cap * 32 + lane;
+    for (uint32_t k = 0; k < n; ++k) P.cand_q[base + (size_t)k * 32] = idx[k];
+  }
+  P.cand_n[d] = (uint8_t)n;
+}
+
+// Grid build shared by both precisions: exclusive scan of the bucket counts, then scatter; with
+// candidate lists also the grid keys (before) and the list rebuild (after), all of them returning
+// at once on steps that need no rebuild.
+template <int D>
 inline void launch_grid_build(const Dev& P, cudaStream_t s, uint64_t* launches) {
   const uint32_t ntiles = cdiv(P.table_total, SCAN_TILE);
+  if (P.cand_q) {
+    k_keys<D><<<cdiv(P.N, 256), 256, 0, s>>>(P);
+    *launches += 1;
+  }
   k_scan_reduce<<<ntiles, SCAN_THREADS, 0, s>>>(P);
   k_scan_final<<<ntiles, SCAN_THREADS, 0, s>>>(P);
   k_scatter<<<cdiv(P.N, 256), 256, 0, s>>>(P);
   *launches += 3;
+  if (P.cand_q) {
+    k_cand_build<D><<<cdiv(P.N, 128), 128, 0, s>>>(P);
+    *launches += 1;
+  }
 }
 
 }  // namespace pg

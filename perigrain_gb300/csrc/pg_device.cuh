@@ -24,6 +24,7 @@ namespace pg {
 
 constexpr uint32_t NONE = 0xffffffffu;
 constexpr int MAX_CAND = 64;        // hard cap of contact candidates held per node
+constexpr uint32_t CAND_CAP = 32;   // candidate-list entries per node (ECAPACITY beyond)
 constexpr int FINAL_THREADS = 1024; // threads of the per-step finalize kernel
 constexpr int WREC_SMEM_CAP = 16384;// wall-reaction records sorted in shared memory per step
 constexpr int FIN_TILE = 2048;       // sorted wall records whose terms are staged in shared memory at once
@@ -65,6 +66,9 @@ struct InstDev {
   float inv_cell_f;     // 1/cell in float (cell coordinates are computed in FP32)
   float cell_f;
   float pre_f;          // FP32 prefilter radius of contact candidates (1.0625 contact_rad)
+  float pre_b;          // candidate lists: FP32 search radius at a build, 1.0625 (R_c + skin)
+  float skin_lim2;      // candidate lists: squared displacement since the last build that forces
+                        // a rebuild, (0.45 skin)^2 (the Verlet bound is skin/2; FP32 margin)
   uint32_t dims[3];     // cells per axis (dims[2] = 1 in 2D)
   uint32_t table_off, table_cap;
   uint32_t node_begin, node_end, grain_begin, grain_end;
@@ -166,6 +170,15 @@ struct Dev {
   uint32_t extforce_maxstep;
   uint32_t max_cand;
   int32_t grain_contact;  // contact parameters from GrainDev (pair mean) instead of InstDev
+  // contact candidate lists (Verlet lists with a skin; cand_q == null: grid search every step).
+  // Node d's candidates are cand_q[(chunk * cand_cap + k) * 32 + lane], k < cand_n[d], in the
+  // reference's visit order; disp_b holds the displacement at the last build (FP32, stride SF);
+  // rebuild != 0 makes this step recount the grid and rebuild the lists.
+  uint32_t* cand_q;
+  uint8_t* cand_n;
+  float* disp_b;
+  uint32_t* rebuild;
+  uint32_t cand_cap;
   int32_t worm;           // run_timeloop_worm semantics (pg_config::timeloop == 1)
   // mask recording (force kernels instantiated with REC = true): per node of this step the
   // offset and count of its active contact entries in rec_ent (entry = partner | friction

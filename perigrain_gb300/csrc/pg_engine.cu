@@ -42,6 +42,15 @@ void enqueue_step(pg_handle* h, int parity, uint64_t* launches) {
   }
 }
 
+// Force a rebuild of the contact candidate lists at the next step (after host writes of state).
+int request_list_rebuild(pg_handle* h) {
+  if (!h->P.rebuild) return PG_OK;
+  const uint32_t one = 1;
+  CU(cudaMemcpyAsync(h->P.rebuild, &one, 4, cudaMemcpyHostToDevice, h->stream));
+  CU(cudaStreamSynchronize(h->stream));
+  return PG_OK;
+}
+
 int build_graphs(pg_handle* h) {
   for (int par = 0; par < 2; ++par) {
     if (h->graph[par]) {
@@ -184,10 +193,12 @@ void pg_config_default(pg_config* c) {
   c->pair_log_capacity = 1024;
   c->first_step = 1;
   c->max_contacts = 48;
+  c->contact_skin = 0.25;
 }
 
 static int validate(const pg_setup_desc* s, const pg_config* c) {
   if (!s || !c) return fail(PG_EINVAL, "null setup or config");
+  if (!(c->contact_skin >= 0) || !std::isfinite(c->contact_skin)) return fail(PG_EINVAL, "contact_skin must be >= 0");
   if (s->dim != 2 && s->dim != 3) return fail(PG_EINVAL, "dim must be 2 or 3");
   if (s->n_instances == 0 || s->n_grains == 0 || s->n_nodes == 0)
     return fail(PG_EINVAL, "empty setup");
@@ -273,10 +284,37 @@ int pg_create(const pg_setup_desc* s, const pg_config* cfg_in, pg_handle** out) 
         best_c = cells[ci];
       }
     }
+  // second stage: the candidate-list skin at the chosen launch shape (0 = grid search every step)
+  double best_skin = cfg_in->contact_skin;
+  {
+    const double skins[] = {0.0, 0.25, 0.5, 1.0};
+    double best_skin_ms = 1e300;
+    for (double sk : skins) {
+      pg_config c = *cfg_in;
+      c.autotune = 0;
+      c.block_size = best_b;
+      c.cells_per_node = best_c;
+      c.contact_skin = sk;
+      c.record_pairs = 0;
+      pg_handle* t = nullptr;
+      int rc = create_impl(s, &c, &t);
+      if (rc) return rc;
+      double ms = 0;
+      rc = pg_step(t, 3);
+      if (!rc) rc = pg_step_timed(t, 24, &ms);
+      pg_destroy(t);
+      if (rc) return rc;
+      if (ms < best_skin_ms) {
+        best_skin_ms = ms;
+        best_skin = sk;
+      }
+    }
+  }
   pg_config c = *cfg_in;
   c.autotune = 0;
   c.block_size = best_b;
   c.cells_per_node = best_c;
+  c.contact_skin = best_skin;
   return create_impl(s, &c, out);
 }
 
@@ -529,8 +567,15 @@ static int create_impl(const pg_setup_desc* s, const pg_config* cfg_in, pg_handl
     }
     double cmin = in.contact_rad * 1.0625;
     if (!(cmin > 0) || !std::isfinite(cmin)) cmin = std::max(ext, 1e-9) / 64;
-    in.cell_min = cmin;
     in.pre_f = (float)cmin;
+    if (cfg.contact_skin > 0) {
+      // candidate lists: cells cover the list radius R_c (1 + skin)
+      cmin *= 1.0 + cfg.contact_skin;
+      const double lim = 0.45 * cfg.contact_skin * in.contact_rad;
+      in.skin_lim2 = (float)(lim * lim);
+    }
+    in.pre_b = (float)cmin;
+    in.cell_min = cmin;
     const uint32_t nn = in.node_end - in.node_begin;
     in.table_cap = (uint32_t)std::max<uint64_t>(1024, (uint64_t)h->L.cells_per_node * nn);
     in.table_off = (uint32_t)table_total;
@@ -584,6 +629,19 @@ static int create_impl(const pg_setup_desc* s, const pg_config* cfg_in, pg_handl
   if (h->precision == PG_MIXED) {
     rc = mixed_setup(h.get(), s);
     if (rc) return rc;
+  }
+  h->contact_skin = cfg.contact_skin;
+  if (cfg.contact_skin > 0) {
+    const uint32_t SF = (D == 2) ? 2 : 4;
+    P.cand_cap = CAND_CAP;
+    CU(h->dalloc(&P.cand_q, (size_t)P.n_chunks * 32 * CAND_CAP));
+    CU(h->dalloc(&P.cand_n, N));
+    CU(h->dalloc(&P.disp_b, (size_t)N * SF));
+    CU(h->dalloc(&P.rebuild, 1));
+    CU(cudaMemset(P.cand_n, 0, N));
+    CU(cudaMemset(P.disp_b, 0, (size_t)N * SF * 4));
+    const uint32_t one = 1;
+    CU(cudaMemcpy(P.rebuild, &one, 4, cudaMemcpyHostToDevice));
   }
   CU(cudaEventCreate(&h->ev_t0));
   CU(cudaEventCreate(&h->ev_t1));
@@ -764,6 +822,8 @@ int pg_set_field(pg_handle* h, int field, const double* in) {
     for (uint32_t c = 0; c < D; ++c) tmp[(size_t)i * S + c] = in[(size_t)i * D + c];
   CU(cudaMemcpy(dst, tmp.data(), tmp.size() * 8, cudaMemcpyHostToDevice));
   if (field == PG_FIELD_DISP) CU(cudaMemset(h->P.clamp_pending, 0, N));
+  rc = request_list_rebuild(h);
+  if (rc) return rc;
   if (h->precision == PG_MIXED && (field == PG_FIELD_DISP || field == PG_FIELD_ACC)) {
     std::vector<float> tf;
     if (field == PG_FIELD_DISP) {
@@ -878,7 +938,7 @@ int pg_set_grain_flags(pg_handle* h, uint32_t grain, int32_t movable, int32_t st
   if (movable >= 0) gd.flags = movable ? (gd.flags | GF_MOVABLE) : (gd.flags & ~GF_MOVABLE);
   if (stoppable >= 0) gd.flags = stoppable ? (gd.flags | GF_STOPPABLE) : (gd.flags & ~GF_STOPPABLE);
   CU(cudaMemcpy(h->P.grain + grain, &gd, sizeof(gd), cudaMemcpyHostToDevice));
-  return PG_OK;
+  return request_list_rebuild(h);
 }
 
 int pg_get_pair_log(pg_handle* h, uint32_t n, uint64_t* count, uint64_t* hash) {
@@ -920,6 +980,12 @@ int pg_get_launch_config(pg_handle* h, uint32_t* block_size, uint32_t* cells_per
   if (!h) return fail(PG_EINVAL, "null handle");
   if (block_size) *block_size = h->L.force_block;
   if (cells_per_node) *cells_per_node = h->L.cells_per_node;
+  return PG_OK;
+}
+
+int pg_get_contact_skin(pg_handle* h, double* skin) {
+  if (!h || !skin) return fail(PG_EINVAL, "null argument");
+  *skin = h->contact_skin;
   return PG_OK;
 }
 

@@ -94,6 +94,12 @@ static int restore_state(pg_handle* h, uint32_t slot) {
   }
   h->vel_parity = G->ckpt_parity[slot];
   h->next_t = G->ckpt_t[slot];
+  // the restored state is not the one the candidate lists were built for (the results do not
+  // depend on when the lists are rebuilt)
+  if (h->P.rebuild) {
+    const uint32_t one = 1;
+    CU(cudaMemcpyAsync(h->P.rebuild, &one, 4, cudaMemcpyHostToDevice, h->stream));
+  }
   return PG_OK;
 }
 

@@ -119,6 +119,7 @@ struct pg_handle {
   pg::LaunchCfg L;
   uint32_t dim = 2, S = 2;
   int precision = PG_FP64;
+  double contact_skin = 0.0;  // candidate-list skin in use (fraction of R_c; 0 = grid search)
   uint64_t next_t = 1;
   int vel_parity = 0;  // 0: current velocity in vel_a
   double* vel_a = nullptr;
@@ -175,3 +176,5 @@ void set_vel(pg_handle* h, pg::Dev& P, int parity);
 void enqueue_step(pg_handle* h, int parity, uint64_t* launches);
 int build_graphs(pg_handle* h);
 int check_device_status(pg_handle* h);
+// Force a rebuild of the contact candidate lists at the next step (no-op without lists).
+int request_list_rebuild(pg_handle* h);

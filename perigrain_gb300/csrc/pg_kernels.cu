@@ -74,8 +74,20 @@ __global__ void __launch_bounds__(256) k_predict(const Dev P) {
       reinterpret_cast<float4*>(P.curf)[d] = make_float4(rf[0], rf[1], rf[2], 0.f);
     }
     const uint32_t key = in.table_off + ((uint32_t)ci[2] * in.dims[1] + (uint32_t)ci[1]) * in.dims[0] + (uint32_t)ci[0];
-    P.cell_key[d] = key;
-    P.cell_rank[d] = atomicAdd(&P.cell_count[key], 1u);
+    if (P.cand_q) {
+      // candidate lists: keys only on rebuild steps (k_keys); rebuild once any node has moved
+      // 0.45 skin since the last build
+      constexpr uint32_t SF = (D == 2) ? 2 : 4;
+      float m2 = 0.f;
+      for (int c = 0; c < D; ++c) {
+        const float dd = (float)dp[c] - P.disp_b[(size_t)d * SF + c];
+        m2 += dd * dd;
+      }
+      if (m2 > in.skin_lim2) *P.rebuild = 1;
+    } else {
+      P.cell_key[d] = key;
+      P.cell_rank[d] = atomicAdd(&P.cell_count[key], 1u);
+    }
     for (int c = 0; c < D; ++c) {
       kmin[c] = dbl_to_ordered(cu[c]);
       kmax[c] = kmin[c];
@@ -192,6 +204,37 @@ __global__ void __launch_bounds__(128) k_force(const Dev P) {
     unsigned long long keys[MAX_CAND];
     uint32_t idx[MAX_CAND];
     int nc = 0;
+    // one candidate q of node d: the FP32 prefilter, the contact rules and the grain-box test,
+    // then insertion in the reference's visit order
+    auto consider = [&](uint32_t q) {
+      float qf[D];
+      ldf<D>(P.curf, q, qf);
+      float d2 = 0.f;
+      for (int c = 0; c < D; ++c) {
+        float dd = qf[c] - pf[c];
+        d2 += dd * dd;
+      }
+      if (d2 > thr2) return;
+      const uint32_t gq = P.node_grain[q];
+      const bool same = (gq == g);
+      if (same ? !selfc : !other) return;
+      if (P.nl_bdry_only && P.bdry_rank[q] == NONE) return;
+      if (!same) {
+        double qmn[D], qmx[D];
+        grain_box<D>(P, gq, qmn, qmx);
+        if (!boxes_touch<D>(bmn, bmx, qmn, qmx, in.contact_rad)) return;
+      }
+      const uint32_t sub = P.nl_bdry_only ? P.bdry_rank[q] : (q - P.grain[gq].node_begin);
+      const unsigned long long key =
+          ((unsigned long long)(same ? 0u : 1u) << 63) | ((unsigned long long)gq << 32) | sub;
+      insert_cand<D>(keys, idx, nc, key, q, P);
+    };
+    if (P.cand_q) {
+      // candidate list of the last rebuild (a superset of the grid search's candidates)
+      const uint32_t ncl = P.cand_n[d];
+      const size_t cbase = (size_t)chunk * P.cand_cap * 32 + lane;
+      for (uint32_t k = 0; k < ncl; ++k) consider(P.cand_q[cbase + (size_t)k * 32]);
+    } else {
     const int z0 = (D == 3) ? max(cc[2] - 1, 0) : 0, z1 = (D == 3) ? min(cc[2] + 1, (int)in.dims[2] - 1) : 0;
     const int y0 = max(cc[1] - 1, 0), y1 = min(cc[1] + 1, (int)in.dims[1] - 1);
     const int x0 = max(cc[0] - 1, 0), x1 = min(cc[0] + 1, (int)in.dims[0] - 1);
@@ -201,30 +244,10 @@ __global__ void __launch_bounds__(128) k_force(const Dev P) {
         const uint32_t b0 = P.cell_start[row + x0], b1 = P.cell_start[row + x1 + 1];
         for (uint32_t b = b0; b < b1; ++b) {
           const uint32_t q = P.sorted[b];
-          if (q == d) continue;
-          float qf[D];
-          ldf<D>(P.curf, q, qf);
-          float d2 = 0.f;
-          for (int c = 0; c < D; ++c) {
-            float dd = qf[c] - pf[c];
-            d2 += dd * dd;
-          }
-          if (d2 > thr2) continue;
-          const uint32_t gq = P.node_grain[q];
-          const bool same = (gq == g);
-          if (same ? !selfc : !other) continue;
-          if (P.nl_bdry_only && P.bdry_rank[q] == NONE) continue;
-          if (!same) {
-            double qmn[D], qmx[D];
-            grain_box<D>(P, gq, qmn, qmx);
-            if (!boxes_touch<D>(bmn, bmx, qmn, qmx, in.contact_rad)) continue;
-          }
-          const uint32_t sub = P.nl_bdry_only ? P.bdry_rank[q] : (q - P.grain[gq].node_begin);
-          const unsigned long long key =
-              ((unsigned long long)(same ? 0u : 1u) << 63) | ((unsigned long long)gq << 32) | sub;
-          insert_cand<D>(keys, idx, nc, key, q, P);
+          if (q != d) consider(q);
         }
       }
+    }
     const uint32_t mydeg = P.node_deg[d];
     for (int ci = 0; ci < nc; ++ci) {
       const uint32_t q = idx[ci];
@@ -510,7 +533,7 @@ static void launch_step_t(const Dev& P, const LaunchCfg& L, cudaStream_t s, uint
   const uint32_t nthr_nodes = P.n_chunks * 32;
   k_predict<D><<<cdiv(P.N, 256), 256, 0, s>>>(P);
   *launches += 1;
-  launch_grid_build(P, s, launches);
+  launch_grid_build<D>(P, s, launches);
   if (P.enable_torque) {
     k_torque_center<D><<<cdiv(P.G, 128), 128, 0, s>>>(P);
     *launches += 1;

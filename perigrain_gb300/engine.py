@@ -18,7 +18,7 @@ class Simulation:
     def __init__(self, setup, dt, enable_fracture=1, nl_bdry_only=0, allow_damping=1, allow_friction=1,
                  self_contact=1, enable_torque=0, gradient_extforce=0, extforce_maxstep=0, precision="fp64",
                  record_pairs=False, pair_log_capacity=1024, first_step=1, max_contacts=48, block_size=0,
-                 autotune=False, cells_per_node=0, timeloop=0):
+                 autotune=False, cells_per_node=0, timeloop=0, contact_skin=0.25):
         L = N.lib()
         self.setup = setup
         self.dim = setup.dim
@@ -42,6 +42,7 @@ class Simulation:
         cfg.autotune = int(bool(autotune))
         cfg.cells_per_node = int(cells_per_node)
         cfg.timeloop = 1 if timeloop in (1, "worm") else 0
+        cfg.contact_skin = float(contact_skin)
         self.cfg = cfg
         self._desc = setup.desc()
         h = C.c_void_p()
@@ -146,6 +147,12 @@ class Simulation:
         tc = C.c_uint64()
         N.check(N.lib().pg_get_device_status(self.h, C.byref(st), C.byref(tc)))
         return st.value, tc.value
+
+    def contact_skin(self):
+        """Candidate-list skin in use (fraction of R_c; 0: grid search every step)."""
+        v = C.c_double()
+        N.check(N.lib().pg_get_contact_skin(self.h, C.byref(v)))
+        return v.value
 
     def launch_count(self):
         n = C.c_uint64()

@@ -34,9 +34,9 @@ def _case(n_grains=6, nodes=120, r=0.3e-3, seed=11):
     return setups.compaction_2d(n_grains=n_grains, r=r, nodes_per_grain=nodes, seed=seed)
 
 
-def _sim(s, precision="fp64"):
+def _sim(s, precision="fp64", contact_skin=0.0):
     return Simulation(s, dt=2e-8, enable_fracture=1, allow_damping=1, allow_friction=1, self_contact=1,
-                      precision=precision)
+                      precision=precision, contact_skin=contact_skin)
 
 
 def _weights(run, frozen, rng):
@@ -83,9 +83,10 @@ def test_replay_reproduces_fp64_engine():
     m.close()
 
 
-def test_product_backward_equals_replay_backward_and_repeats():
+@pytest.mark.parametrize("skin", [0.0, 0.5])
+def test_product_backward_equals_replay_backward_and_repeats(skin):
     s = _case(seed=12)
-    sim = _sim(s)
+    sim = _sim(s, contact_skin=skin)
     run = grad.GradRun(sim, 300, checkpoint_every=40)
     m = run.record_masks()
     rng = np.random.default_rng(0)
