@@ -295,6 +295,38 @@ int pg_build_bonds_noalloc(const double* pos, uint32_t n, uint32_t dim, double d
                            uint64_t capacity, uint64_t* n_pairs, void* stream);
 const char* pg_noalloc_last_error(void);
 
+/* Incircle packing of a simplex mesh: the grain centres and radii the reference's packing
+ * generator computes from its mesh (exp_dict.py:1072-1313 get_incenter_mesh_loc; the mesher,
+ * gmsh, is the caller's). All arrays are device pointers. */
+typedef struct pg_pack_mesh {
+  uint32_t dim;               /* 2: triangles, 3: tetrahedra */
+  uint32_t n_nodes;
+  uint32_t n_elems;
+  const double* pos;          /* [n_nodes][dim] */
+  const uint32_t* elems;      /* [n_elems][dim + 1] node indices */
+  uint32_t n_bdry_nodes;
+  const uint32_t* bdry_nodes; /* [n_bdry_nodes] */
+  uint32_t n_bdry_edges;      /* 2D boundary segments (used by the maximin pass with gen_bdry) */
+  const uint32_t* bdry_edges; /* [n_bdry_edges][2] */
+} pg_pack_mesh;
+
+/* Writes the incircle (insphere) of every element -- centres[e], radii[e] for e < n_elems --
+ * followed by one circle per mesh node in node order (exp_dict.py:1186-1296):
+ *   modify_nodal_circles == 0: interior nodes; centre = the node, radius = min over the node's
+ *     elements of |incenter - node| - inradius (2D and 3D);
+ *   modify_nodal_circles != 0 (2D only): interior nodes, plus boundary nodes when gen_bdry; the
+ *     solution of the reference's per-node maximin problem (the largest circle clear of the
+ *     surrounding incircles and, for boundary nodes, of the lines of their boundary edges,
+ *     centred in the box of those incircles' centres), reached from the reference's initial guess.
+ * centers: [n_elems + n_nodes][dim] doubles, radii: [n_elems + n_nodes]; *n_out receives the number
+ * of circles written. *n_unpolished (may be NULL) counts maximin nodes whose exact solve found no
+ * tight point (their circle is the ascent's end point). Temporary device memory is allocated and
+ * freed inside the call; runs on `stream` and returns after it completes.
+ * pg_pack_last_error() describes a failure. */
+int pg_pack_incenters(const pg_pack_mesh* mesh, int32_t modify_nodal_circles, int32_t gen_bdry, double* centers,
+                      double* radii, uint32_t* n_out, uint32_t* n_unpolished, void* stream);
+const char* pg_pack_last_error(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -69,6 +69,12 @@ CONF_FIELDS = [
 ]
 
 
+class PackMesh(C.Structure):
+    _fields_ = [("dim", C.c_uint32), ("n_nodes", C.c_uint32), ("n_elems", C.c_uint32), ("pos", C.c_void_p),
+                ("elems", C.c_void_p), ("n_bdry_nodes", C.c_uint32), ("bdry_nodes", C.c_void_p),
+                ("n_bdry_edges", C.c_uint32), ("bdry_edges", C.c_void_p)]
+
+
 class Post(C.Structure):
     _fields_ = [(k, f64p) for k in ("grain_mean_vel", "grain_mean_acc", "grain_mean_currpos", "grain_force",
                                     "grain_damage", "node_damage", "inertial_force", "volume_fraction")]
@@ -115,6 +121,9 @@ PROTOTYPES = [
                                          u64p, C.c_void_p]),
     ("pg_noalloc_last_error", C.c_char_p, []),
     ("pg_postprocess", C.c_int, [C.c_void_p, C.c_void_p]),
+    ("pg_pack_incenters", C.c_int, [C.POINTER(PackMesh), C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, u32p, u32p,
+                                    C.c_void_p]),
+    ("pg_pack_last_error", C.c_char_p, []),
     # gradients
     ("pg_set_grain_params", C.c_int, [C.c_void_p, f64p, f64p, f64p, f64p, f64p]),
     ("pg_get_grain_params", C.c_int, [C.c_void_p, f64p, f64p, f64p, f64p, f64p]),

@@ -22,7 +22,7 @@ namespace pg {
 constexpr int BT = 256;               // threads per block
 constexpr int SCAN_T = 1024;          // scan block
 constexpr int SCAN_TILE_B = SCAN_T * 4;
-constexpr int MAX_PARTNERS = 512;     // partners j > i held per node while sorting
+constexpr int MAX_PARTNERS = 4096;    // partners j > i of one node (the row is sorted in place)
 
 struct BondGrid {
   double origin[3];
@@ -135,16 +135,13 @@ __global__ void kb_scatter(uint32_t n, BondScratch S) {
   if (i < n) S.sorted[S.cell_start[S.key[i]] + S.rank[i]] = i;
 }
 
-template <bool WRITE>
-__global__ void kb_pairs(const double* pos, uint32_t n, uint32_t dim, double delta, BondGrid g, BondScratch S,
-                         uint32_t* pairs, uint64_t capacity) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+// Visit every partner j > i of node i within delta, in the grid's cell order: f(j).
+template <class F>
+__device__ __forceinline__ void for_partners(const double* pos, uint32_t i, uint32_t dim, double delta,
+                                             const BondGrid& g, const BondScratch& S, F f) {
   int32_t cc[3];
   const double* pi = pos + (size_t)i * dim;
   bond_cell_of(pi, dim, g, cc);
-  uint32_t mine[WRITE ? MAX_PARTNERS : 1];
-  uint32_t cnt = 0;
   const int z0 = dim == 3 ? max(cc[2] - 1, 0) : 0, z1 = dim == 3 ? min(cc[2] + 1, (int)g.dims[2] - 1) : 0;
   const int y0 = max(cc[1] - 1, 0), y1 = min(cc[1] + 1, (int)g.dims[1] - 1);
   const int x0 = max(cc[0] - 1, 0), x1 = min(cc[0] + 1, (int)g.dims[0] - 1);
@@ -159,31 +156,56 @@ __global__ void kb_pairs(const double* pos, uint32_t n, uint32_t dim, double del
         double s = (pj[0] - pi[0]) * (pj[0] - pi[0]);
         for (uint32_t c = 1; c < dim; ++c) s = s + (pj[c] - pi[c]) * (pj[c] - pi[c]);
         if (!(sqrt(s) <= delta)) continue;
-        if (WRITE) {
-          if (cnt < MAX_PARTNERS) {
-            uint32_t k = cnt;
-            while (k > 0 && mine[k - 1] > j) {
-              mine[k] = mine[k - 1];
-              --k;
-            }
-            mine[k] = j;
-          } else {
-            atomicCAS(S.error, 0, (int32_t)PG_ECAPACITY);
-          }
-        }
-        ++cnt;
+        f(j);
       }
     }
+}
+
+// WRITE = false: count node i's partners j > i. WRITE = true: write row i (pairs (i, j), j
+// ascending) at its offset: the partners go to the row in visit order and are sorted there; a row
+// that crosses `capacity` gets its smallest partners that fit, picked one at a time.
+template <bool WRITE>
+__global__ void kb_pairs(const double* pos, uint32_t n, uint32_t dim, double delta, BondGrid g, BondScratch S,
+                         uint32_t* pairs, uint64_t capacity) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
   if (!WRITE) {
+    uint32_t cnt = 0;
+    for_partners(pos, i, dim, delta, g, S, [&](uint32_t) { ++cnt; });
     S.pcount[i] = cnt;
+    if (cnt > (uint32_t)MAX_PARTNERS) atomicCAS(S.error, 0, (int32_t)PG_ECAPACITY);
     return;
   }
   const uint64_t off = S.poff[i];
-  const uint32_t m = cnt < MAX_PARTNERS ? cnt : MAX_PARTNERS;
-  for (uint32_t k = 0; k < m; ++k) {
-    if (off + k < capacity) {
-      pairs[2 * (off + k)] = i;
-      pairs[2 * (off + k) + 1] = mine[k];
+  const uint32_t cnt = S.pcount[i];
+  if (cnt == 0 || off >= capacity) return;
+  if (off + cnt <= capacity) {
+    uint32_t k = 0;
+    for_partners(pos, i, dim, delta, g, S, [&](uint32_t j) {
+      if (k < cnt) pairs[2 * (off + k) + 1] = j;
+      ++k;
+    });
+    // insertion sort of the row by j
+    for (uint32_t a = 1; a < cnt; ++a) {
+      const uint32_t v = pairs[2 * (off + a) + 1];
+      uint32_t b = a;
+      while (b > 0 && pairs[2 * (off + b - 1) + 1] > v) {
+        pairs[2 * (off + b) + 1] = pairs[2 * (off + b - 1) + 1];
+        --b;
+      }
+      pairs[2 * (off + b) + 1] = v;
+    }
+    for (uint32_t a = 0; a < cnt; ++a) pairs[2 * (off + a)] = i;
+  } else {
+    uint32_t prev = i;
+    for (uint64_t k = off; k < capacity; ++k) {
+      uint32_t best = 0xffffffffu;
+      for_partners(pos, i, dim, delta, g, S, [&](uint32_t j) {
+        if (j > prev && j < best) best = j;
+      });
+      pairs[2 * k] = i;
+      pairs[2 * k + 1] = best;
+      prev = best;
     }
   }
 }
@@ -195,6 +217,14 @@ static cudaError_t scan_u32(const uint32_t* in, uint32_t len, uint32_t* out, con
   const uint32_t tiles = cdivb(len ? len : 1, SCAN_TILE_B);
   kb_scan_tiles<<<tiles, SCAN_T, 0, st>>>(in, len, S.tile_sum, S.done);
   kb_scan_final<<<tiles, SCAN_T, 0, st>>>(in, len, S.tile_sum, out);
+  return cudaGetLastError();
+}
+
+cudaError_t scan_u32_dev(const uint32_t* in, uint32_t len, uint32_t* out, uint32_t* tile_sum, uint32_t* done,
+                         cudaStream_t st) {
+  const uint32_t tiles = cdivb(len ? len : 1, SCAN_TILE_B);
+  kb_scan_tiles<<<tiles, SCAN_T, 0, st>>>(in, len, tile_sum, done);
+  kb_scan_final<<<tiles, SCAN_T, 0, st>>>(in, len, tile_sum, out);
   return cudaGetLastError();
 }
 
@@ -284,7 +314,7 @@ int run_bond_build(const double* pos, uint32_t n, uint32_t dim, double delta, ui
   }
   *n_pairs = total;
   if (derr) {
-    *err = "a node has more than 512 partners j > i within delta";
+    *err = "a node has more than 4096 partners j > i within delta";
     return PG_ECAPACITY;
   }
   if (total > capacity) {

@@ -24,6 +24,10 @@ struct BondScratch {
 };
 
 uint32_t bond_grid_cells(uint32_t n);
+// Exclusive scan of in[0..len) into out[0..len], out[len] = total, on stream st. tile_sum holds
+// bond_scan_tiles(len) words; *done must be 0 (and is 0 again when the scan ends).
+cudaError_t scan_u32_dev(const uint32_t* in, uint32_t len, uint32_t* out, uint32_t* tile_sum, uint32_t* done,
+                         cudaStream_t st);
 uint32_t bond_scan_tiles(uint32_t len);
 int run_bond_build(const double* pos, uint32_t n, uint32_t dim, double delta, uint32_t* pairs, uint64_t capacity,
                    uint64_t* n_pairs, cudaStream_t st, const BondScratch& S, std::string* err);

@@ -554,8 +554,16 @@ static void launch_step_t(const Dev& P, const LaunchCfg& L, cudaStream_t s, uint
 
 cudaError_t kernels_init() {
   cudaError_t e = cudaFuncSetAttribute(k_finalize<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, FINAL_SMEM);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_finalize<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, FINAL_SMEM);
   if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(k_finalize<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, FINAL_SMEM);
+  // the recording variants of the force kernel have local frames of about 1.1 KB
+  const void* fs[] = {(const void*)k_force<2, false, false>, (const void*)k_force<2, false, true>,
+                      (const void*)k_force<2, true, false>,  (const void*)k_force<2, true, true>,
+                      (const void*)k_force<3, false, false>, (const void*)k_force<3, false, true>,
+                      (const void*)k_force<3, true, false>,  (const void*)k_force<3, true, true>};
+  size_t need = 0;
+  e = max_local_bytes(fs, 8, &need);
+  return e == cudaSuccess ? ensure_local_bytes(need) : e;
 }
 
 void launch_step(const Dev& P, const LaunchCfg& L, cudaStream_t s, uint64_t* launches, bool rec) {

@@ -13,6 +13,27 @@ struct LaunchCfg {
   uint32_t cells_per_node = 4;  // grid capacity per node of an instance
 };
 
+// Per-thread local memory of this process's context at least `bytes` (cudaLimitStackSize), so
+// kernels with local frames above the default limit find room for them.
+inline cudaError_t ensure_local_bytes(size_t bytes) {
+  size_t cur = 0;
+  cudaError_t e = cudaDeviceGetLimit(&cur, cudaLimitStackSize);
+  if (e != cudaSuccess || cur >= bytes) return e;
+  return cudaDeviceSetLimit(cudaLimitStackSize, (bytes + 255) / 256 * 256);
+}
+// The largest local frame (cudaFuncAttributes::localSizeBytes) among the kernels `fs`.
+inline cudaError_t max_local_bytes(const void* const* fs, int n, size_t* out) {
+  size_t m = 0;
+  for (int k = 0; k < n; ++k) {
+    cudaFuncAttributes a;
+    const cudaError_t e = cudaFuncGetAttributes(&a, fs[k]);
+    if (e != cudaSuccess) return e;
+    m = a.localSizeBytes > m ? a.localSizeBytes : m;
+  }
+  *out = m;
+  return cudaSuccess;
+}
+
 cudaError_t kernels_init();
 // Enqueue one FP64 time step on stream s. Adds the number of kernel launches to *launches. With
 // rec the force kernel also records the step's contact and wall masks (Dev::rec_*).

@@ -738,8 +738,16 @@ static void launch_mx(const Dev& P, const LaunchCfg& L, cudaStream_t s, uint64_t
 
 cudaError_t kernels_mixed_init() {
   cudaError_t e = cudaFuncSetAttribute(k_finalize<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, FINAL_SMEM);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_finalize<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, FINAL_SMEM);
   if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(k_finalize<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, FINAL_SMEM);
+  // the recording variants of the force kernel have local frames of about 1.1 KB
+  const void* fs[] = {(const void*)k_force_mx<2, false, false>, (const void*)k_force_mx<2, false, true>,
+                      (const void*)k_force_mx<2, true, false>,  (const void*)k_force_mx<2, true, true>,
+                      (const void*)k_force_mx<3, false, false>, (const void*)k_force_mx<3, false, true>,
+                      (const void*)k_force_mx<3, true, false>,  (const void*)k_force_mx<3, true, true>};
+  size_t need = 0;
+  e = max_local_bytes(fs, 8, &need);
+  return e == cudaSuccess ? ensure_local_bytes(need) : e;
 }
 
 void launch_step_mixed(const Dev& P, const LaunchCfg& L, cudaStream_t s, uint64_t* launches, cudaEvent_t e0,
