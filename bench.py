@@ -252,6 +252,46 @@ def adjoint_bench(n_steps=5000, checkpoint_every=100, n_fd=4):
                     "their gradients) separate and h=1e-4 differences are nonlinear"}
 
 
+def packing_bench(nx=800, ny=500, repeats=3):
+    """Incircle packing (pg_pack_incenters) of a jittered 800 x 500-cell triangulated rectangle with
+    the reference's default options (maximin nodal circles, boundary nodes included): circles per
+    second with the mesh resident in HBM, end to end from host arrays, and the oracle's scalar CPU
+    port on a bounded sample (the reference solves each node's model with GEKKO, not installed)."""
+    import torch
+
+    from perigrain_gb300 import packing
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import packing_oracle as PO
+
+    m = packing.rect_mesh(nx, ny, width=nx * 1e-4, height=ny * 1e-4, jitter=0.25, seed=21)
+    d_pos = torch.from_numpy(m.pos).cuda()
+    d_T, d_bn, d_be = packing._u32(m.T), packing._u32(m.bdry_nodes), packing._u32(m.bdry_edges)
+    packing.pack_device(d_pos, d_T, d_bn, d_be)  # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(repeats):
+        cen, rad, unp = packing.pack_device(d_pos, d_T, d_bn, d_be)
+    dev_s = (time.perf_counter() - t0) / repeats
+    n_circ = int(rad.shape[0])
+    t0 = time.perf_counter()
+    out = packing.get_incenter_mesh_loc(m)
+    e2e_s = time.perf_counter() - t0
+    sm = packing.rect_mesh(40, 25, width=40e-4, height=25e-4, jitter=0.25, seed=22)
+    t0 = time.perf_counter()
+    _, crad, _ = PO.incenter_mesh_loc(sm.pos, sm.T, sm.bdry_nodes, sm.bdry_edges, True, True)
+    cpu_s = time.perf_counter() - t0
+    return {"workload": "rect mesh %d x %d cells, %d nodes, %d triangles, maximin nodal circles with boundary nodes"
+                        % (nx, ny, len(m.pos), len(m.T)),
+            "metric": "circles/s", "value": n_circ / dev_s, "ms": dev_s * 1e3, "circles": n_circ,
+            "unpolished": unp, "packing_ratio": float(out.packing_ratio()),
+            "e2e": {"value": n_circ / e2e_s, "unit": "circles/s",
+                    "note": "host mesh -> device, pg_pack_incenters, circles -> host"},
+            "cpu_baseline": {"value": len(crad) / cpu_s, "unit": "circles/s", "cores": 1, "kind": "port",
+                             "sample": "oracle scalar port on a 40 x 25-cell mesh (%d circles), %.2f s"
+                                       % (len(crad), cpu_s)}}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -262,9 +302,12 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=400)
     ap.add_argument("--no-adjoint", action="store_true", help="skip the gradient-path measurement")
+    ap.add_argument("--no-packing", action="store_true", help="skip the packing-generator measurement")
     ap.add_argument("--profile-adjoint", type=int, default=0, metavar="STEPS",
                     help="only a forward + backward of STEPS steps of the differentiable compaction "
                          "(checkpoint every 100; the command profiled under ncu)")
+    ap.add_argument("--profile-packing", type=int, default=0, metavar="NX",
+                    help="only incircle packings of an NX x 0.625 NX-cell mesh (the command profiled under ncu)")
     ap.add_argument("--profile-run", action="store_true",
                     help="only warmup + steps of the engine (the command profiled under ncu)")
     a = ap.parse_args()
@@ -291,6 +334,21 @@ def main():
 
     import perigrain_gb300 as pg
     from perigrain_gb300 import Simulation
+
+    if a.profile_packing:
+        import torch
+
+        from perigrain_gb300 import packing
+
+        nx = a.profile_packing
+        m = packing.rect_mesh(nx, nx * 5 // 8, width=nx * 1e-4, height=nx * 5 // 8 * 1e-4, jitter=0.25, seed=21)
+        d_pos = torch.from_numpy(m.pos).cuda()
+        d_T, d_bn, d_be = packing._u32(m.T), packing._u32(m.bdry_nodes), packing._u32(m.bdry_edges)
+        for _ in range(a.warmup + a.steps):
+            cen, rad, unp = packing.pack_device(d_pos, d_T, d_bn, d_be)
+        print("profile packing: %d nodes, %d triangles, %d circles, unpolished %d, %d calls"
+              % (len(m.pos), len(m.T), rad.shape[0], unp, a.warmup + a.steps))
+        return
 
     if a.profile_adjoint:
         from perigrain_gb300 import grad, setups
@@ -431,6 +489,7 @@ def main():
     traffic = profiled_traffic("%s/%s" % (spec["name"], a.precision))
     cpu_v, cpu_info = cpu_reference(setup, spec, a.cpu_steps, threads)
     adjoint = None if a.no_adjoint else adjoint_bench()
+    packing_line = None if a.no_packing else packing_bench()
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": ms_max / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -460,6 +519,7 @@ def main():
         "sequential_fp64": seq,
         "accuracy": accuracy,
         "adjoint": adjoint,
+        "packing": packing_line,
     }
     print(json.dumps(line), flush=True)
     if dist:

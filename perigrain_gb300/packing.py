@@ -72,19 +72,19 @@ def rect_mesh(nx, ny, width=1.0, height=1.0, jitter=0.2, seed=0):
     x = np.where(inner, x + rng.uniform(-jitter, jitter, x.shape) * hx, x)
     y = np.where(inner, y + rng.uniform(-jitter, jitter, y.shape) * hy, y)
     pos = np.stack([x.ravel(), y.ravel()], axis=1)
+    ci, cj = np.meshgrid(np.arange(nx), np.arange(ny), indexing="xy")
+    ci, cj = ci.ravel(), cj.ravel()  # cells in row-major order (j outer, i inner)
+    a = cj * (nx + 1) + ci
+    b, c, d = a + 1, a + nx + 2, a + nx + 1
+    even = (ci + cj) % 2 == 0
+    t1 = np.where(even[:, None], np.stack([a, b, c], 1), np.stack([a, b, d], 1))
+    t2 = np.where(even[:, None], np.stack([a, c, d], 1), np.stack([b, c, d], 1))
+    T = np.stack([t1, t2], 1).reshape(-1, 3)
     idx = lambda i, j: j * (nx + 1) + i
-    T = []
-    for j in range(ny):
-        for i in range(nx):
-            a, b, c, d = idx(i, j), idx(i + 1, j), idx(i + 1, j + 1), idx(i, j + 1)
-            if (i + j) % 2 == 0:
-                T += [(a, b, c), (a, c, d)]
-            else:
-                T += [(a, b, d), (b, c, d)]
-    ring = ([idx(i, 0) for i in range(nx)] + [idx(nx, j) for j in range(ny)] +
-            [idx(i, ny) for i in range(nx, 0, -1)] + [idx(0, j) for j in range(ny, 0, -1)])
-    edges = [(ring[k], ring[(k + 1) % len(ring)]) for k in range(len(ring))]
-    return PackMesh(pos, np.array(T, np.int64), ring, np.array(edges, np.int64))
+    ring = np.concatenate([idx(np.arange(nx), 0), idx(nx, np.arange(ny)), idx(np.arange(nx, 0, -1), ny),
+                           idx(0, np.arange(ny, 0, -1))])
+    edges = np.stack([ring, np.roll(ring, -1)], 1)
+    return PackMesh(pos, T, ring, edges)
 
 
 def cube_mesh(n, size=1.0, jitter=0.2, seed=0):
@@ -187,37 +187,42 @@ def _u32(a, cols=None):
     return torch.from_numpy(a.astype(np.uint32).view(np.int32)).cuda()
 
 
-def get_incenter_mesh_loc(mesh, modify_nodal_circles=True, gen_bdry=True, stream=None):
-    """Incircle packing of `mesh` on the GPU; returns an IncenterNodes whose incircle_rad has
-    shape [count, 1] like the reference's. modify_nodal_circles needs a 2D mesh."""
+def pack_device(d_pos, d_T, d_bdry_nodes, d_bdry_edges, modify_nodal_circles=True, gen_bdry=True, stream=None):
+    """pg_pack_incenters on device tensors (float64 [n, dim]; int32 views of uint32 indices);
+    returns (centres [k, dim], radii [k], unpolished) as device tensors."""
     import torch
 
-    dim = mesh.dim
-    nn, ne = len(mesh.pos), len(mesh.T)
-    d_pos = torch.from_numpy(mesh.pos).cuda()
-    d_T = _u32(mesh.T)
-    d_bn = _u32(mesh.bdry_nodes)
-    be = mesh.bdry_edges if dim == 2 else np.zeros((0, 2), np.int64)
-    d_be = _u32(be)
+    nn, dim = d_pos.shape
+    ne = d_T.shape[0]
     total = ne + nn
-    d_cen = torch.empty((max(total, 1), dim), dtype=torch.float64, device="cuda")
-    d_rad = torch.empty(max(total, 1), dtype=torch.float64, device="cuda")
+    d_cen = torch.empty((max(total, 1), dim), dtype=torch.float64, device=d_pos.device)
+    d_rad = torch.empty(max(total, 1), dtype=torch.float64, device=d_pos.device)
     m = N.PackMesh()
     m.dim, m.n_nodes, m.n_elems = dim, nn, ne
     m.pos = C.c_void_p(d_pos.data_ptr())
     m.elems = C.c_void_p(d_T.data_ptr())
-    m.n_bdry_nodes = len(mesh.bdry_nodes)
-    m.bdry_nodes = C.c_void_p(d_bn.data_ptr() if len(mesh.bdry_nodes) else 0)
-    m.n_bdry_edges = len(be)
-    m.bdry_edges = C.c_void_p(d_be.data_ptr() if len(be) else 0)
+    m.n_bdry_nodes = d_bdry_nodes.numel()
+    m.bdry_nodes = C.c_void_p(d_bdry_nodes.data_ptr() if d_bdry_nodes.numel() else 0)
+    m.n_bdry_edges = d_bdry_edges.shape[0] if d_bdry_edges.numel() else 0
+    m.bdry_edges = C.c_void_p(d_bdry_edges.data_ptr() if d_bdry_edges.numel() else 0)
     n_out, unp = C.c_uint32(), C.c_uint32()
-    torch.cuda.synchronize()
     rc = N.lib().pg_pack_incenters(C.byref(m), int(bool(modify_nodal_circles)), int(bool(gen_bdry)),
                                    C.c_void_p(d_cen.data_ptr()), C.c_void_p(d_rad.data_ptr()), C.byref(n_out),
                                    C.byref(unp), stream)
     if rc != N.PG_OK:
         raise N.PerigrainError(rc, N.lib().pg_pack_last_error().decode())
     k = n_out.value
-    cen = d_cen[:k].cpu().numpy()
-    rad = d_rad[:k].cpu().numpy()[:, None]
-    return IncenterNodes(cen, rad, mesh, unp.value)
+    return d_cen[:k], d_rad[:k], unp.value
+
+
+def get_incenter_mesh_loc(mesh, modify_nodal_circles=True, gen_bdry=True, stream=None):
+    """Incircle packing of `mesh` on the GPU; returns an IncenterNodes whose incircle_rad has
+    shape [count, 1] like the reference's. modify_nodal_circles needs a 2D mesh."""
+    import torch
+
+    be = mesh.bdry_edges if mesh.dim == 2 else np.zeros((0, 2), np.int64)
+    d_pos = torch.from_numpy(mesh.pos).cuda()
+    d_T, d_bn, d_be = _u32(mesh.T), _u32(mesh.bdry_nodes), _u32(be.reshape(-1, 2))
+    torch.cuda.synchronize()
+    d_cen, d_rad, unp = pack_device(d_pos, d_T, d_bn, d_be, modify_nodal_circles, gen_bdry, stream)
+    return IncenterNodes(d_cen.cpu().numpy(), d_rad.cpu().numpy()[:, None], mesh, unp)
