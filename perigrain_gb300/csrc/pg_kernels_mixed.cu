@@ -173,12 +173,21 @@ __global__ void __launch_bounds__(256) k_predict_mx(const Dev P) {
   uint32_t g = 0;
   unsigned long long kmin[D], kmax[D];
   if (act) {
+    // every per-node load is issued before the grain's flags are known, so they overlap
     g = P.node_grain[d];
-    const GrainDev& gr = P.grain[g];
-    double dp[D], ps[D], cu[D];
+    double dp[D], ps[D], cu[D], v[D];
+    float a[D];
     ldv<D>(P.disp, d, dp);
+    ldv<D>(P.vel_in, d, v);
+    ldvf<D>(P.acc_f, d, a);
+    ldv<D>(P.pos, d, ps);
+    constexpr uint32_t SFB = (D == 2) ? 2 : 4;
+    float db[D];
+    for (int c = 0; c < D; ++c) db[c] = P.cand_q ? P.disp_b[(size_t)d * SFB + c] : 0.f;
+    const bool pend = P.clamp_pending[d] != 0;
+    const GrainDev& gr = P.grain[g];
     bool wrote = false;
-    if (P.clamp_pending[d]) {
+    if (pend) {
       for (int c = 0; c < D; ++c) dp[c] = 0.0;
       P.clamp_pending[d] = 0;
       wrote = true;
@@ -186,10 +195,7 @@ __global__ void __launch_bounds__(256) k_predict_mx(const Dev P) {
     if (gr.flags & GF_MOVABLE) {
       // the increment dt*v + (dt*dt/2)*a is formed in FP32 (relative error ~1e-7 of a step's
       // motion); the accumulation into disp stays FP64
-      double v[D], vd;
-      float a[D];
-      ldv<D>(P.vel_in, d, v);
-      ldvf<D>(P.acc_f, d, a);
+      double vd;
       for (int c = 0; c < D; ++c) {
         const float vf = trunc_f32(v[c], &vd);
         dp[c] = dp[c] + widen(fmaf(P.dt_f, vf, P.hdt2_f * a[c]));
@@ -200,7 +206,6 @@ __global__ void __launch_bounds__(256) k_predict_mx(const Dev P) {
       stv<D>(P.disp, d, dp);
       st_ref_disp<D>(P.bref, P.N, d, dp);
     }
-    ldv<D>(P.pos, d, ps);
     for (int c = 0; c < D; ++c) cu[c] = ps[c] + dp[c];
     stv<D>(P.cur, d, cu);
     const InstDev& in = P.inst[gr.inst];
@@ -233,10 +238,9 @@ __global__ void __launch_bounds__(256) k_predict_mx(const Dev P) {
     if (P.cand_q) {
       // candidate lists: keys only on rebuild steps (k_keys); rebuild once any node has moved
       // 0.45 skin since the last build
-      constexpr uint32_t SF = (D == 2) ? 2 : 4;
       float m2 = 0.f;
       for (int c = 0; c < D; ++c) {
-        const float dd = (float)dp[c] - P.disp_b[(size_t)d * SF + c];
+        const float dd = (float)dp[c] - db[c];
         m2 += dd * dd;
       }
       if (m2 > in.skin_lim2) *P.rebuild = 1;
@@ -342,15 +346,36 @@ __global__ void __launch_bounds__(128) k_force_mx(const Dev P) {
         }
       }
     }
+    // the alive words and neighbour indices of the next pair are loaded one iteration ahead, so
+    // only the neighbour gathers wait on memory in each iteration
+    uint32_t wa_n = 0u, wb_n = 0u, ca_n = d, cb_n = d;
+    if (cdeg > 0) {
+      wa_n = P.alive[w0];
+      ca_n = P.bcol[slot0];
+    }
+    if (cdeg > 1) {
+      wb_n = P.alive[w0 + 1];
+      cb_n = P.bcol[slot0 + 32u];
+    }
     for (uint32_t k = 0; k < cdeg; k += 2) {
       const bool two = (k + 1) < cdeg;
-      const uint32_t wa = P.alive[w0 + k];
-      const uint32_t wb = two ? P.alive[w0 + k + 1] : 0u;
+      const uint32_t wa = wa_n, wb = wb_n, ca = ca_n, cb = cb_n;
+      if (k + 2 < cdeg) {
+        wa_n = P.alive[w0 + k + 2];
+        ca_n = P.bcol[slot0 + 32u * (k + 2)];
+      }
+      if (k + 3 < cdeg) {
+        wb_n = P.alive[w0 + k + 3];
+        cb_n = P.bcol[slot0 + 32u * (k + 3)];
+      } else {
+        wb_n = 0u;
+        cb_n = d;
+      }
       bool ba = (wa >> lane) & 1u, bb = (wb >> lane) & 1u;
       const bool ua = mov && ba, ub = mov && bb;
       const uint32_t sa = slot0 + 32u * k, sb = sa + 32u;
-      const uint32_t ja = ua ? P.bcol[sa] : d;
-      const uint32_t jb = ub ? P.bcol[sb] : d;
+      const uint32_t ja = ua ? ca : d;
+      const uint32_t jb = ub ? cb : d;
       float adh[D], adl[D], axh[D], axl[D], bdh[D], bdl[D], bxh[D], bxl[D];
       ld_ref<D>(P.bref, P.N, ja, adh, adl, axh, axl);
       ld_ref<D>(P.bref, P.N, jb, bdh, bdl, bxh, bxl);
