@@ -428,13 +428,13 @@ __global__ void __launch_bounds__(128) k_force_mx(const Dev P) {
     auto consider = [&](uint32_t q) {
       float qf[D];
       ldf<D>(P.curf, q, qf);
+      const uint32_t gq = P.node_grain[q];  // issued with the position, used after the prefilter
       float d2 = 0.f;
       for (int c = 0; c < D; ++c) {
         float dd = qf[c] - ph[c];
         d2 = fmaf(dd, dd, d2);
       }
       if (d2 > thr2) return;
-      const uint32_t gq = P.node_grain[q];
       const bool same = (gq == g);
       if (same ? !selfc : !other) return;
       if (P.nl_bdry_only && P.bdry_rank[q] == NONE) return;
@@ -452,7 +452,12 @@ __global__ void __launch_bounds__(128) k_force_mx(const Dev P) {
       // candidate list of the last rebuild (a superset of the grid search's candidates)
       const uint32_t ncl = P.cand_n[d];
       const size_t cbase = (size_t)chunk * P.cand_cap * 32 + lane;
-      for (uint32_t k = 0; k < ncl; ++k) consider(P.cand_q[cbase + (size_t)k * 32]);
+      uint32_t qn = ncl ? P.cand_q[cbase] : d;  // the next entry is loaded one candidate ahead
+      for (uint32_t k = 0; k < ncl; ++k) {
+        const uint32_t q = qn;
+        if (k + 1 < ncl) qn = P.cand_q[cbase + (size_t)(k + 1) * 32];
+        consider(q);
+      }
     } else {
     const int z0 = (D == 3) ? max(cc[2] - 1, 0) : 0, z1 = (D == 3) ? min(cc[2] + 1, (int)in.dims[2] - 1) : 0;
     const int y0 = max(cc[1] - 1, 0), y1 = min(cc[1] + 1, (int)in.dims[1] - 1);
