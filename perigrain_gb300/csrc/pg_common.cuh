@@ -57,6 +57,34 @@ __device__ __forceinline__ void ldf(const float* a, uint32_t i, float (&v)[D]) {
 
 __device__ __forceinline__ void set_status(int32_t* st, int32_t code) { atomicCAS(st, 0, code); }
 
+// Programmatic dependent launch. Every kernel of a step starts with pdl_enter(), which waits until
+// the previous kernel in the stream has finished and its writes are visible; launched with
+// programmatic stream serialization, the kernel's blocks are scheduled while the previous kernel's
+// last blocks drain instead of after it. (No early launch_dependents: letting the next kernel's
+// blocks in while the current one still runs measured slower.) A no-op for a kernel launched
+// without the attribute.
+__device__ __forceinline__ void pdl_enter() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+// Launch k<<<g, b, smem, s>>>(args...), with programmatic stream serialization when `pdl`.
+template <class... KArgs, class... Args>
+inline void launch_k(void (*k)(KArgs...), dim3 g, dim3 b, size_t smem, cudaStream_t s, bool pdl, Args... args) {
+  if (!pdl) {
+    k<<<g, b, smem, s>>>(args...);
+    return;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = g;
+  cfg.blockDim = b;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, k, args...);
+}
+
 // Mask recording: append this node's contact entries to rec_ent (one atomic per warp; the whole
 // warp must call this) and store its offset, count and wall bits. On overflow of rec_cap the
 // node's list is stored empty and PG_ECAPACITY raised, so the host can grow the buffer and redo.
@@ -152,6 +180,7 @@ __device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* warp_s
 __device__ __forceinline__ bool grid_idle(const Dev& P) { return P.cand_q && !*P.rebuild; }
 
 static __global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(const Dev P) {
+  pdl_enter();
   __shared__ uint32_t ws[32];
   __shared__ bool last;
   if (grid_idle(P)) return;
@@ -197,6 +226,7 @@ static __global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(const Dev P
 }
 
 static __global__ void __launch_bounds__(SCAN_THREADS) k_scan_final(const Dev P) {
+  pdl_enter();
   __shared__ uint32_t ws[32];
   if (grid_idle(P)) return;
   const uint32_t tile = blockIdx.x;
@@ -245,6 +275,7 @@ static __global__ void __launch_bounds__(SCAN_THREADS) k_scan_final(const Dev P)
 }
 
 static __global__ void __launch_bounds__(256) k_scatter(const Dev P) {
+  pdl_enter();
   if (grid_idle(P)) return;
   const uint32_t d = blockIdx.x * blockDim.x + threadIdx.x;
   if (d < P.N) P.sorted[P.cell_start[P.cell_key[d]] + P.cell_rank[d]] = d;
@@ -255,6 +286,7 @@ static __global__ void __launch_bounds__(256) k_scatter(const Dev P) {
 // ---------------------------------------------------------------------------------------------
 template <int D>
 static __global__ void k_torque_center(const Dev P) {
+  pdl_enter();
   const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= P.G) return;
   const GrainDev gr = P.grain[g];
@@ -324,6 +356,7 @@ __device__ __forceinline__ void insert_cand(unsigned long long (&keys)[MAX_CAND]
 // ---------------------------------------------------------------------------------------------
 template <int D>
 static __global__ void __launch_bounds__(FINAL_THREADS) k_finalize(const Dev P) {
+  pdl_enter();
   extern __shared__ unsigned long long skey[];
   constexpr int NS = 2 * D;
   const uint32_t tid = threadIdx.x;
@@ -478,6 +511,7 @@ inline uint32_t cdiv(uint32_t a, uint32_t b) { return (a + b - 1) / b; }
 // grid keys of a rebuild step (the grid-search path computes them in the predict kernels)
 template <int D>
 static __global__ void __launch_bounds__(256) k_keys(const Dev P) {
+  pdl_enter();
   if (!*P.rebuild) return;
   const uint32_t d = blockIdx.x * blockDim.x + threadIdx.x;
   if (d >= P.N) return;
@@ -497,6 +531,7 @@ static __global__ void __launch_bounds__(256) k_keys(const Dev P) {
 // The bounding-box prefilter is applied per step, not here. Also records the displacement.
 template <int D>
 static __global__ void __launch_bounds__(128) k_cand_build(const Dev P) {
+  pdl_enter();
   if (!*P.rebuild) return;
   const uint32_t d = blockIdx.x * blockDim.x + threadIdx.x;
   if (d >= P.N) return;
@@ -570,18 +605,18 @@ static __global__ void __launch_bounds__(128) k_cand_build(const Dev P) {
 // candidate lists also the grid keys (before) and the list rebuild (after), all of them returning
 // at once on steps that need no rebuild.
 template <int D>
-inline void launch_grid_build(const Dev& P, cudaStream_t s, uint64_t* launches) {
+inline void launch_grid_build(const Dev& P, cudaStream_t s, uint64_t* launches, bool pdl = false) {
   const uint32_t ntiles = cdiv(P.table_total, SCAN_TILE);
   if (P.cand_q) {
-    k_keys<D><<<cdiv(P.N, 256), 256, 0, s>>>(P);
+    launch_k(k_keys<D>, cdiv(P.N, 256), 256, 0, s, pdl, P);
     *launches += 1;
   }
-  k_scan_reduce<<<ntiles, SCAN_THREADS, 0, s>>>(P);
-  k_scan_final<<<ntiles, SCAN_THREADS, 0, s>>>(P);
-  k_scatter<<<cdiv(P.N, 256), 256, 0, s>>>(P);
+  launch_k(k_scan_reduce, ntiles, SCAN_THREADS, 0, s, pdl, P);
+  launch_k(k_scan_final, ntiles, SCAN_THREADS, 0, s, pdl, P);
+  launch_k(k_scatter, cdiv(P.N, 256), 256, 0, s, pdl, P);
   *launches += 3;
   if (P.cand_q) {
-    k_cand_build<D><<<cdiv(P.N, 128), 128, 0, s>>>(P);
+    launch_k(k_cand_build<D>, cdiv(P.N, 128), 128, 0, s, pdl, P);
     *launches += 1;
   }
 }

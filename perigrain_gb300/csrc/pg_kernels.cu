@@ -28,6 +28,7 @@ namespace pg {
 // ---------------------------------------------------------------------------------------------
 template <int D>
 __global__ void __launch_bounds__(256) k_predict(const Dev P) {
+  pdl_enter();
   const uint32_t d = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t lane = threadIdx.x & 31;
   const bool act = d < P.N;
@@ -125,6 +126,7 @@ __global__ void __launch_bounds__(256) k_predict(const Dev P) {
 
 template <int D, bool REC, bool GC>
 __global__ void __launch_bounds__(128) k_force(const Dev P) {
+  pdl_enter();
   const uint32_t d = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t chunk = d >> 5;
@@ -531,24 +533,27 @@ template <int D>
 static void launch_step_t(const Dev& P, const LaunchCfg& L, cudaStream_t s, uint64_t* launches,
                           cudaEvent_t e0 = nullptr, cudaEvent_t e1 = nullptr, bool rec = false) {
   const uint32_t nthr_nodes = P.n_chunks * 32;
-  k_predict<D><<<cdiv(P.N, 256), 256, 0, s>>>(P);
+  // programmatic dependent launch between the kernels of a step, except where events are
+  // recorded between them (timed mode)
+  const bool pdl = !e0 && !e1;
+  launch_k(k_predict<D>, cdiv(P.N, 256), 256, 0, s, pdl, P);
   *launches += 1;
-  launch_grid_build<D>(P, s, launches);
+  launch_grid_build<D>(P, s, launches, pdl);
   if (P.enable_torque) {
-    k_torque_center<D><<<cdiv(P.G, 128), 128, 0, s>>>(P);
+    launch_k(k_torque_center<D>, cdiv(P.G, 128), 128, 0, s, pdl, P);
     *launches += 1;
   }
   if (e0) cudaEventRecord(e0, s);
   const dim3 grid(cdiv(nthr_nodes, L.force_block)), block(L.force_block);
   if (P.grain_contact) {
-    if (rec) k_force<D, true, true><<<grid, block, 0, s>>>(P);
-    else k_force<D, false, true><<<grid, block, 0, s>>>(P);
+    if (rec) launch_k(k_force<D, true, true>, grid, block, 0, s, pdl, P);
+    else launch_k(k_force<D, false, true>, grid, block, 0, s, pdl, P);
   } else {
-    if (rec) k_force<D, true, false><<<grid, block, 0, s>>>(P);
-    else k_force<D, false, false><<<grid, block, 0, s>>>(P);
+    if (rec) launch_k(k_force<D, true, false>, grid, block, 0, s, pdl, P);
+    else launch_k(k_force<D, false, false>, grid, block, 0, s, pdl, P);
   }
   if (e1) cudaEventRecord(e1, s);
-  k_finalize<D><<<1, FINAL_THREADS, FINAL_SMEM, s>>>(P);
+  launch_k(k_finalize<D>, 1, FINAL_THREADS, FINAL_SMEM, s, pdl, P);
   *launches += 2;
 }
 

@@ -167,6 +167,7 @@ __device__ __forceinline__ float dotf(const float (&a)[D], const float (&b)[D]) 
 // ---------------------------------------------------------------------------------------------
 template <int D>
 __global__ void __launch_bounds__(256) k_predict_mx(const Dev P) {
+  pdl_enter();
   const uint32_t d = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t lane = threadIdx.x & 31;
   const bool act = d < P.N;
@@ -309,6 +310,7 @@ __device__ __forceinline__ void bond_term(const float (&dh)[D], const float (&dl
 // ---------------------------------------------------------------------------------------------
 template <int D, bool REC, bool GC>
 __global__ void __launch_bounds__(128) k_force_mx(const Dev P) {
+  pdl_enter();
   const uint32_t d = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t chunk = d >> 5;
@@ -743,11 +745,14 @@ template <int D>
 static void launch_mx(const Dev& P, const LaunchCfg& L, cudaStream_t s, uint64_t* launches, cudaEvent_t e0,
                       cudaEvent_t e1, bool rec) {
   const uint32_t nthr = P.n_chunks * 32;
-  k_predict_mx<D><<<cdiv(P.N, 256), 256, 0, s>>>(P);
+  // programmatic dependent launch between the kernels of a step, except where events are
+  // recorded between them (timed mode)
+  const bool pdl = !e0 && !e1;
+  launch_k(k_predict_mx<D>, cdiv(P.N, 256), 256, 0, s, pdl, P);
   *launches += 1;
-  launch_grid_build<D>(P, s, launches);
+  launch_grid_build<D>(P, s, launches, pdl);
   if (P.enable_torque) {
-    k_torque_center<D><<<cdiv(P.G, 128), 128, 0, s>>>(P);
+    launch_k(k_torque_center<D>, cdiv(P.G, 128), 128, 0, s, pdl, P);
     *launches += 1;
   }
   if (e0) cudaEventRecord(e0, s);
@@ -755,14 +760,14 @@ static void launch_mx(const Dev& P, const LaunchCfg& L, cudaStream_t s, uint64_t
   // where used, so the plain kernel keeps its register budget
   const dim3 grid(cdiv(nthr, L.force_block)), block(L.force_block);
   if (P.grain_contact) {
-    if (rec) k_force_mx<D, true, true><<<grid, block, 0, s>>>(P);
-    else k_force_mx<D, false, true><<<grid, block, 0, s>>>(P);
+    if (rec) launch_k(k_force_mx<D, true, true>, grid, block, 0, s, pdl, P);
+    else launch_k(k_force_mx<D, false, true>, grid, block, 0, s, pdl, P);
   } else {
-    if (rec) k_force_mx<D, true, false><<<grid, block, 0, s>>>(P);
-    else k_force_mx<D, false, false><<<grid, block, 0, s>>>(P);
+    if (rec) launch_k(k_force_mx<D, true, false>, grid, block, 0, s, pdl, P);
+    else launch_k(k_force_mx<D, false, false>, grid, block, 0, s, pdl, P);
   }
   if (e1) cudaEventRecord(e1, s);
-  k_finalize<D><<<1, FINAL_THREADS, FINAL_SMEM, s>>>(P);
+  launch_k(k_finalize<D>, 1, FINAL_THREADS, FINAL_SMEM, s, pdl, P);
   *launches += 2;
 }
 
