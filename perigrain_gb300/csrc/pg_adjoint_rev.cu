@@ -220,6 +220,7 @@ __device__ __forceinline__ void stfv(float* a, uint32_t i, const float (&v)[D]) 
 // s = (2 xi.et + et.et) / (|xi| (|xi + et| + |xi|)), force cotangents from the FP32 array fbf.
 template <int D, bool F32>
 __global__ void __launch_bounds__(32 * SUB) k_adj_bonds(const Dev P, const AdjStep A) {
+  pdl_enter();
   __shared__ double red[SUB][D + 1][32];
   const uint32_t lane = threadIdx.x & 31, sub = threadIdx.x >> 5;
   const uint32_t chunk = blockIdx.x;
@@ -335,6 +336,7 @@ __global__ void __launch_bounds__(32 * SUB) k_adj_bonds(const Dev P, const AdjSt
 // of the next reverse step to fbf.
 template <int D>
 __global__ void __launch_bounds__(32 * SUB) k_adj_rest(const Dev P, const AdjStep A) {
+  pdl_enter();
   constexpr int NS = 2 * D;
   constexpr int NV = 2 * D + NPARAM;  // xb[D], vfb[D], pc[NPARAM]
   __shared__ double red[SUB][NV][32];
@@ -558,6 +560,7 @@ __global__ void __launch_bounds__(32 * SUB) k_adj_rest(const Dev P, const AdjSte
 // force cotangents of the first reverse step from the seed cotangent (FP32 bond path)
 template <int D>
 __global__ void k_fb_init(const Dev P, const AdjStep A) {
+  pdl_enter();
   const uint32_t d = blockIdx.x * blockDim.x + threadIdx.x;
   if (d >= P.N) return;
   double Fb[D];
@@ -586,14 +589,16 @@ __global__ void __launch_bounds__(256) k_grad_reduce(const Dev P, const double* 
 }
 
 void launch_adjoint_step(const Dev& P, const AdjStep& A, cudaStream_t s, uint64_t* launches) {
+  // programmatic dependent launch: each kernel waits on its predecessor in pdl_enter()
+  const dim3 g(P.n_chunks), b(32 * SUB);
   if (P.dim == 2) {
-    if (A.fbf) k_adj_bonds<2, true><<<P.n_chunks, 32 * SUB, 0, s>>>(P, A);
-    else k_adj_bonds<2, false><<<P.n_chunks, 32 * SUB, 0, s>>>(P, A);
-    k_adj_rest<2><<<P.n_chunks, 32 * SUB, 0, s>>>(P, A);
+    if (A.fbf) launch_k(k_adj_bonds<2, true>, g, b, 0, s, true, P, A);
+    else launch_k(k_adj_bonds<2, false>, g, b, 0, s, true, P, A);
+    launch_k(k_adj_rest<2>, g, b, 0, s, true, P, A);
   } else {
-    if (A.fbf) k_adj_bonds<3, true><<<P.n_chunks, 32 * SUB, 0, s>>>(P, A);
-    else k_adj_bonds<3, false><<<P.n_chunks, 32 * SUB, 0, s>>>(P, A);
-    k_adj_rest<3><<<P.n_chunks, 32 * SUB, 0, s>>>(P, A);
+    if (A.fbf) launch_k(k_adj_bonds<3, true>, g, b, 0, s, true, P, A);
+    else launch_k(k_adj_bonds<3, false>, g, b, 0, s, true, P, A);
+    launch_k(k_adj_rest<3>, g, b, 0, s, true, P, A);
   }
   *launches += 2;
 }
@@ -601,9 +606,9 @@ void launch_adjoint_step(const Dev& P, const AdjStep& A, cudaStream_t s, uint64_
 void launch_fb_init(const Dev& P, const AdjStep& A, cudaStream_t s, uint64_t* launches) {
   const uint32_t nb = (P.N + 127) / 128;
   if (P.dim == 2) {
-    k_fb_init<2><<<nb, 128, 0, s>>>(P, A);
+    launch_k(k_fb_init<2>, nb, 128, 0, s, true, P, A);
   } else {
-    k_fb_init<3><<<nb, 128, 0, s>>>(P, A);
+    launch_k(k_fb_init<3>, nb, 128, 0, s, true, P, A);
   }
   *launches += 1;
 }
