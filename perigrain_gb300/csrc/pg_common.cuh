@@ -352,11 +352,81 @@ __device__ __forceinline__ void insert_cand(unsigned long long (&keys)[MAX_CAND]
 }
 
 // ---------------------------------------------------------------------------------------------
-// k_finalize: one block. Wall reactions in node order, pair log, wall move, step counter.
+// Per-instance end of a step (blocks 1.. of k_finalize, one warp per instance): wall move
+// (timeloop.h:866-878); the instance's grid refitted to this step's bounding box for the next step
+// (the grain boxes of the predict kernel folded by the warp, then reset for the next step).
+constexpr uint32_t FINAL_BLOCK_INSTANCES = 64;  // up to this many instances: a block each, else a warp each
+
+inline uint32_t finalize_blocks(uint32_t I) {
+  return 1 + (I <= FINAL_BLOCK_INSTANCES ? I : (I + FINAL_THREADS / 32 - 1) / (FINAL_THREADS / 32));
+}
+
+template <int D>
+__device__ __forceinline__ void finalize_instances(const Dev& P) {
+  constexpr int NS = 2 * D;
+  __shared__ unsigned long long red[2 * D][FINAL_THREADS / 32];
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const bool per_block = P.I <= FINAL_BLOCK_INSTANCES;
+  const uint32_t k = per_block ? blockIdx.x - 1 : (blockIdx.x - 1) * (blockDim.x >> 5) + warp;
+  if (k >= P.I) return;
+  InstDev* in = &P.inst[k];
+  const uint32_t r = per_block ? threadIdx.x : lane, nr = per_block ? blockDim.x : 32u;
+  if (r < (uint32_t)NS) in->wall[r] = in->wall[r] + in->wall_speed[r] * P.dt;
+  unsigned long long mn[D], mx[D];
+  for (int c = 0; c < D; ++c) {
+    mn[c] = ~0ull;
+    mx[c] = 0ull;
+  }
+  const uint32_t gb = in->grain_begin, ge = in->grain_end;
+  for (uint32_t g = gb + r; g < ge; g += nr) {
+    for (int c = 0; c < D; ++c) {
+      const unsigned long long a = P.bbox[(size_t)g * NS + c], b = P.bbox[(size_t)g * NS + D + c];
+      mn[c] = a < mn[c] ? a : mn[c];
+      mx[c] = b > mx[c] ? b : mx[c];
+      P.bbox[(size_t)g * NS + c] = ~0ull;
+      P.bbox[(size_t)g * NS + D + c] = 0ull;
+    }
+  }
+  for (int c = 0; c < D; ++c) {
+    mn[c] = warp_min_u64(mn[c]);
+    mx[c] = warp_max_u64(mx[c]);
+  }
+  if (per_block) {
+    if (lane == 0)
+      for (int c = 0; c < D; ++c) {
+        red[c][warp] = mn[c];
+        red[D + c][warp] = mx[c];
+      }
+    __syncthreads();
+    if (warp != 0) return;
+    const uint32_t nw = blockDim.x >> 5;
+    for (int c = 0; c < D; ++c) {
+      mn[c] = warp_min_u64(lane < nw ? red[c][lane] : ~0ull);
+      mx[c] = warp_max_u64(lane < nw ? red[D + c][lane] : 0ull);
+    }
+  }
+  if (lane == 0) {
+    double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+    bool ok = ge > gb;
+    for (int c = 0; c < D; ++c) {
+      lo[c] = ordered_to_dbl(mn[c]);
+      hi[c] = ordered_to_dbl(mx[c]);
+      ok = ok && isfinite(lo[c]) && isfinite(hi[c]);
+    }
+    if (ok) fit_grid(*in, D, lo, hi);
+  }
+}
+
+// k_finalize, block 0: wall reactions in node order, pair log, step counter; blocks 1..: one warp
+// per instance (finalize_instances).
 // ---------------------------------------------------------------------------------------------
 template <int D>
 static __global__ void __launch_bounds__(FINAL_THREADS) k_finalize(const Dev P) {
   pdl_enter();
+  if (blockIdx.x > 0) {
+    finalize_instances<D>(P);
+    return;
+  }
   extern __shared__ unsigned long long skey[];
   constexpr int NS = 2 * D;
   const uint32_t tid = threadIdx.x;
@@ -463,38 +533,6 @@ static __global__ void __launch_bounds__(FINAL_THREADS) k_finalize(const Dev P) 
     *P.wrec_count = 0;
     *P.step = t + 1;
     if (P.cand_q) *P.rebuild = 0;
-  }
-  for (uint32_t p = tid; p < P.I * NS; p += blockDim.x) {
-    InstDev* in = &P.inst[p / NS];
-    const int s = p % NS;
-    in->wall[s] = in->wall[s] + in->wall_speed[s] * P.dt;
-  }
-  // refit every instance's grid to this step's bounding box for the next step: grain boxes are
-  // folded into per-instance boxes (one atomic per grain and bound), then one thread per instance
-  for (uint32_t g = tid; g < P.G; g += blockDim.x) {
-    const uint32_t k = P.grain[g].inst;
-    for (int c = 0; c < D; ++c) {
-      atomicMin(&P.ibox[(size_t)k * NS + c], P.bbox[(size_t)g * NS + c]);
-      atomicMax(&P.ibox[(size_t)k * NS + D + c], P.bbox[(size_t)g * NS + D + c]);
-    }
-  }
-  __syncthreads();
-  for (uint32_t k = tid; k < P.I; k += blockDim.x) {
-    InstDev* in = &P.inst[k];
-    double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
-    bool ok = in->grain_end > in->grain_begin;
-    for (int c = 0; c < D; ++c) {
-      lo[c] = ordered_to_dbl(__ldcg(&P.ibox[(size_t)k * NS + c]));  // atomics live in L2
-      hi[c] = ordered_to_dbl(__ldcg(&P.ibox[(size_t)k * NS + D + c]));
-      ok = ok && isfinite(lo[c]) && isfinite(hi[c]);
-      P.ibox[(size_t)k * NS + c] = ~0ull;
-      P.ibox[(size_t)k * NS + D + c] = 0ull;
-    }
-    if (ok) fit_grid(*in, D, lo, hi);
-  }
-  __syncthreads();
-  for (uint32_t i = tid; i < P.G * NS; i += blockDim.x) {
-    P.bbox[i] = ((i % NS) < (uint32_t)D) ? ~0ull : 0ull;
   }
 }
 
