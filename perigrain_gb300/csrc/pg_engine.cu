@@ -4,8 +4,10 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <string>
@@ -318,12 +320,60 @@ int pg_create(const pg_setup_desc* s, const pg_config* cfg_in, pg_handle** out) 
   return create_impl(s, &c, out);
 }
 
+// SELL-32 bond slab from the reference CSR, one warp per chunk of 32 nodes (lane = node): bond k of
+// node 32c + lane goes to slot chunk_slot[c] + 32k + lane with its global neighbour index and
+// xi_norm = |pos[j] - pos[i]| (gen_xi, particle2.h:236-252; the FP64 operations of the reference,
+// this file is compiled without contraction); slots past a node's degree hold index 0 and norm 1;
+// alive word (c, k) has bit lane set for k < degree.
+__global__ void k_layout_bonds(const double* pos, uint32_t S, uint32_t D, uint32_t N, const uint64_t* off,
+                               const uint32_t* loc, const uint32_t* grain_node_offset, const uint32_t* node_grain,
+                               const uint32_t* chunk_slot, const uint32_t* chunk_word, const uint32_t* chunk_deg,
+                               uint32_t* bcol, double* bxin, uint32_t* alive) {
+  const uint32_t c = blockIdx.x, lane = threadIdx.x, i = c * 32 + lane;
+  const bool act = i < N;
+  const uint32_t deg = act ? (uint32_t)(off[i + 1] - off[i]) : 0u;
+  const uint32_t n0 = act ? grain_node_offset[node_grain[i]] : 0u;
+  const uint32_t cd = chunk_deg[c];
+  for (uint32_t k = 0; k < cd; ++k) {
+    const size_t sl = chunk_slot[c] + (size_t)k * 32 + lane;
+    const bool has = k < deg;
+    uint32_t j = 0;
+    double xn = 1.0;
+    if (has) {
+      j = n0 + loc[off[i] + k];
+      double xi[3] = {0.0, 0.0, 0.0};
+      for (uint32_t a = 0; a < D; ++a) xi[a] = pos[(size_t)j * S + a] - pos[(size_t)i * S + a];
+      double n2 = xi[0] * xi[0];
+      for (uint32_t a = 1; a < D; ++a) n2 = n2 + xi[a] * xi[a];
+      xn = sqrt(n2);
+    }
+    bcol[sl] = j;
+    bxin[sl] = xn;
+    const uint32_t w = __ballot_sync(0xffffffffu, has);
+    if (lane == 0) alive[chunk_word[c] + k] = w;
+  }
+}
+
+// Phase times of pg_create on stderr (host wall clock) when the environment sets PERIGRAIN_TRACE.
+struct CreateTrace {
+  bool on = std::getenv("PERIGRAIN_TRACE") != nullptr;
+  std::chrono::steady_clock::time_point t = std::chrono::steady_clock::now();
+  void mark(const char* what) {
+    if (!on) return;
+    const auto n = std::chrono::steady_clock::now();
+    std::fprintf(stderr, "pg_create %-22s %9.2f ms\n", what, std::chrono::duration<double, std::milli>(n - t).count());
+    t = n;
+  }
+};
+
 static int create_impl(const pg_setup_desc* s, const pg_config* cfg_in, pg_handle** out) {
   if (!out) return fail(PG_EINVAL, "null out");
   *out = nullptr;
+  CreateTrace tr;
   pg_config cfg = *cfg_in;
   int rc = validate(s, &cfg);
   if (rc) return rc;
+  tr.mark("validate");
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(PG_ENODEV, "no CUDA device");
   if (cfg.pair_log_capacity == 0) cfg.pair_log_capacity = 1024;
@@ -337,6 +387,7 @@ static int create_impl(const pg_setup_desc* s, const pg_config* cfg_in, pg_handl
   std::unique_ptr<pg_handle> h(new pg_handle);
   CU(cudaGetDevice(&h->device));
   CU(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+  tr.mark("context and stream");
   const uint32_t D = s->dim, S = (D == 2) ? 2 : 4, N = s->n_nodes, G = s->n_grains, I = s->n_instances;
   h->dim = D;
   h->S = S;
@@ -402,6 +453,7 @@ static int create_impl(const pg_setup_desc* s, const pg_config* cfg_in, pg_handl
   CU(cudaMemcpy(P.extf, tmp.data(), tmp.size() * 8, cudaMemcpyHostToDevice));
   CU(cudaMemset(P.force, 0, tmp.size() * 8));
   CU(cudaMemcpy(P.vol, s->vol, (size_t)N * 8, cudaMemcpyHostToDevice));
+  tr.mark("node vectors");
 
   // ---- per node metadata ----
   std::vector<uint32_t> node_grain(N), bdry_rank(N, NONE);
@@ -424,6 +476,7 @@ static int create_impl(const pg_setup_desc* s, const pg_config* cfg_in, pg_handl
   CU(cudaMemcpy(P.bdry_rank, bdry_rank.data(), N * 4, cudaMemcpyHostToDevice));
   CU(cudaMemcpy(P.clamped, clamped.data(), N, cudaMemcpyHostToDevice));
   CU(cudaMemset(P.clamp_pending, 0, N));
+  tr.mark("node classes");
 
   // ---- bonds: reference CSR -> SELL-32 ----
   const uint32_t NC = P.n_chunks;
@@ -445,25 +498,6 @@ static int create_impl(const pg_setup_desc* s, const pg_config* cfg_in, pg_handl
   h->chunk_slot[NC] = (uint32_t)slots;
   h->chunk_word[NC] = (uint32_t)words;
   if (slots >= (1ull << 32)) return fail(PG_EINVAL, "bond slab too large");
-  std::vector<uint32_t> bcol(slots, 0), alive(words, 0);
-  std::vector<double> bxin(slots, 1.0);
-  for (uint32_t i = 0; i < N; ++i) {
-    const uint32_t g = node_grain[i], n0 = s->grain_node_offset[g];
-    const uint32_t c = i >> 5, lane = i & 31;
-    for (uint32_t k = 0; k < h->node_deg[i]; ++k) {
-      const uint64_t b = s->bond_offset[i] + k;
-      const uint32_t j = n0 + s->bond_local[b];
-      const size_t sl = h->chunk_slot[c] + (size_t)k * 32 + lane;
-      bcol[sl] = j;
-      // gen_xi (particle2.h:236-252): xi = pos[j] - pos[i]; xi_norm = |xi|
-      double xi[3];
-      for (uint32_t a = 0; a < D; ++a) xi[a] = s->pos[(size_t)j * D + a] - s->pos[(size_t)i * D + a];
-      double n2 = xi[0] * xi[0];
-      for (uint32_t a = 1; a < D; ++a) n2 = n2 + xi[a] * xi[a];
-      bxin[sl] = std::sqrt(n2);
-      alive[h->chunk_word[c] + k] |= (1u << lane);
-    }
-  }
   CU(h->dalloc(&P.chunk_slot, NC + 1));
   CU(h->dalloc(&P.chunk_word, NC + 1));
   CU(h->dalloc(&P.chunk_deg, NC));
@@ -477,11 +511,31 @@ static int create_impl(const pg_setup_desc* s, const pg_config* cfg_in, pg_handl
   CU(cudaMemcpy(P.chunk_deg, chunk_deg.data(), NC * 4, cudaMemcpyHostToDevice));
   CU(cudaMemcpy(P.node_deg, h->node_deg.data(), N * 4, cudaMemcpyHostToDevice));
   if (slots) {
-    CU(cudaMemcpy(P.bcol, bcol.data(), slots * 4, cudaMemcpyHostToDevice));
-    CU(cudaMemcpy(P.bxin, bxin.data(), slots * 8, cudaMemcpyHostToDevice));
-    CU(cudaMemset(P.break_step, 0, slots * 4));
+    // the reference CSR goes up once; the SELL-32 slab, the alive words and xi_norm are built on
+    // the device
+    const uint64_t nb = s->bond_offset[N];
+    uint64_t* d_off = nullptr;
+    uint32_t* d_loc = nullptr;
+    uint32_t* d_gno = nullptr;
+    cudaError_t e = cudaMalloc((void**)&d_off, (size_t)(N + 1) * 8);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&d_loc, (size_t)std::max<uint64_t>(nb, 1) * 4);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&d_gno, (size_t)(G + 1) * 4);
+    if (e == cudaSuccess) e = cudaMemcpy(d_off, s->bond_offset, (size_t)(N + 1) * 8, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && nb) e = cudaMemcpy(d_loc, s->bond_local, (size_t)nb * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d_gno, s->grain_node_offset, (size_t)(G + 1) * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+      k_layout_bonds<<<NC, 32>>>(P.pos, S, D, N, d_off, d_loc, d_gno, P.node_grain, P.chunk_slot, P.chunk_word,
+                                 P.chunk_deg, P.bcol, P.bxin, P.alive);
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemset(P.break_step, 0, slots * 4);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    cudaFree(d_off);
+    cudaFree(d_loc);
+    cudaFree(d_gno);
+    CU(e);
   }
-  if (words) CU(cudaMemcpy(P.alive, alive.data(), words * 4, cudaMemcpyHostToDevice));
+  tr.mark("bond layout");
 
   // ---- grains ----
   std::vector<GrainDev> grains(G);
@@ -606,6 +660,7 @@ static int create_impl(const pg_setup_desc* s, const pg_config* cfg_in, pg_handl
   CU(h->dalloc(&P.scan_tile_sum, ntiles));
   CU(h->dalloc(&P.scan_done, 1));
   CU(cudaMemset(P.scan_done, 0, 4));
+  tr.mark("grains, grid");
 
   // ---- wall records, logs, control ----
   P.wrec_cap = (uint32_t)std::min<uint64_t>(WREC_SMEM_CAP, 2ull * D * N);
@@ -626,9 +681,11 @@ static int create_impl(const pg_setup_desc* s, const pg_config* cfg_in, pg_handl
   CU(cudaMemset(P.status, 0, 4));
   CU(h->dalloc(&P.too_close, 1));
   CU(cudaMemset(P.too_close, 0, 8));
+  tr.mark("logs and control");
   if (h->precision == PG_MIXED) {
     rc = mixed_setup(h.get(), s);
     if (rc) return rc;
+    tr.mark("mixed images");
   }
   h->contact_skin = cfg.contact_skin;
   if (cfg.contact_skin > 0) {
@@ -646,8 +703,10 @@ static int create_impl(const pg_setup_desc* s, const pg_config* cfg_in, pg_handl
   CU(cudaEventCreate(&h->ev_t0));
   CU(cudaEventCreate(&h->ev_t1));
   CU(cudaDeviceSynchronize());
+  tr.mark("lists, sync");
   rc = build_graphs(h.get());
   if (rc) return rc;
+  tr.mark("graphs");
   *out = h.release();
   return PG_OK;
 }
