@@ -99,6 +99,33 @@ static void pack_f(const double* x, uint32_t N, uint32_t D, std::vector<float>* 
     for (uint32_t c = 0; c < D; ++c) (*out)[(size_t)i * SF + c] = (float)x[(size_t)i * D + c];
 }
 
+// FP32 images of the uploaded FP64 state for the mixed path (the host packing of pack_hl/pack_f,
+// same conversions): bref = [disp hi, disp lo, (pos - xorigin) hi, lo] per node (2D record, 3D
+// planes), acc, extforce and vol in FP32.
+__global__ void k_mixed_images(const Dev P) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P.N) return;
+  const uint32_t D = P.dim, S = (D == 2) ? 2 : 4, SF = S, N = P.N;
+  const InstDev& in = P.inst[P.grain[P.node_grain[i]].inst];
+  for (uint32_t c = 0; c < D; ++c) {
+    const double dv = P.disp[(size_t)i * S + c];
+    const float dh = (float)dv, dl = (float)(dv - (double)dh);
+    const double xv = P.pos[(size_t)i * S + c] - in.xorigin[c];
+    const float xh = (float)xv, xl = (float)(xv - (double)xh);
+    const float q4[4] = {dh, dl, xh, xl};
+    for (uint32_t q = 0; q < 4; ++q) {
+      if (D == 2) {
+        P.bref[(size_t)i * 8 + q * 2 + c] = q4[q];
+      } else {
+        P.bref[(size_t)(q * D + c) * N + i] = q4[q];
+      }
+    }
+    P.acc_f[(size_t)i * SF + c] = (float)P.acc[(size_t)i * S + c];
+    P.extf_f[(size_t)i * SF + c] = (float)P.extf[(size_t)i * S + c];
+  }
+  P.vol_f[i] = (float)P.vol[i];
+}
+
 static int mixed_setup(pg_handle* h, const pg_setup_desc* s) {
   Dev& P = h->P;
   const uint32_t N = P.N, D = h->dim, SF = (D == 2) ? 2 : 4;
@@ -111,38 +138,15 @@ static int mixed_setup(pg_handle* h, const pg_setup_desc* s) {
   P.dt_f = (float)P.dt;
   P.hdt2_f = (float)P.hdt2;
   P.half_dt_f = (float)P.half_dt;
-  std::vector<double> org((size_t)N * 3, 0.0);
-  for (uint32_t g = 0; g < P.G; ++g) {
-    const InstDev& in = h->inst_host[s->grain_instance[g]];
-    for (uint32_t i = s->grain_node_offset[g]; i < s->grain_node_offset[g + 1]; ++i)
-      for (uint32_t c = 0; c < 3; ++c) org[(size_t)i * 3 + c] = in.xorigin[c];
-  }
-  std::vector<float> tmp, xr, ref((size_t)N * 4 * D, 0.f);
-  pack_hl(s->disp, N, D, nullptr, &tmp);
-  pack_hl(s->pos, N, D, &org, &xr);
-  // 2D: per-node record [disp hi, disp lo, xpos hi, xpos lo]; 3D: planes in that order
-  for (uint32_t i = 0; i < N; ++i)
-    for (uint32_t c = 0; c < D; ++c) {
-      const float v[4] = {tmp[(size_t)i * 2 * SF + c], tmp[(size_t)i * 2 * SF + SF + c], xr[(size_t)i * 2 * SF + c],
-                          xr[(size_t)i * 2 * SF + SF + c]};
-      for (uint32_t q = 0; q < 4; ++q) {
-        if (D == 2) {
-          ref[(size_t)i * 8 + q * 2 + c] = v[q];
-        } else {
-          ref[(size_t)(q * D + c) * N + i] = v[q];
-        }
-      }
-    }
-  CU(cudaMemcpy(P.bref, ref.data(), ref.size() * 4, cudaMemcpyHostToDevice));
+  (void)s;
   CU(cudaMemset(P.cur_hl, 0, (size_t)N * 2 * SF * 4));
-  pack_f(s->acc, N, D, &tmp);
-  CU(cudaMemcpy(P.acc_f, tmp.data(), tmp.size() * 4, cudaMemcpyHostToDevice));
-  pack_f(s->extforce, N, D, &tmp);
-  CU(cudaMemcpy(P.extf_f, tmp.data(), tmp.size() * 4, cudaMemcpyHostToDevice));
+  CU(cudaMemset(P.acc_f, 0, (size_t)N * SF * 4));
+  CU(cudaMemset(P.extf_f, 0, (size_t)N * SF * 4));
   CU(cudaMemset(P.force_f, 0, (size_t)N * SF * 4));
-  std::vector<float> v(N);
-  for (uint32_t i = 0; i < N; ++i) v[i] = (float)s->vol[i];
-  CU(cudaMemcpy(P.vol_f, v.data(), (size_t)N * 4, cudaMemcpyHostToDevice));
+  if (N) {
+    k_mixed_images<<<(N + 255) / 256, 256>>>(P);
+    CU(cudaGetLastError());
+  }
   return PG_OK;
 }
 
@@ -320,6 +324,12 @@ int pg_create(const pg_setup_desc* s, const pg_config* cfg_in, pg_handle** out) 
   return create_impl(s, &c, out);
 }
 
+// out[k] = a[k] + b[k]
+__global__ void k_add_vec(const double* a, const double* b, double* out, uint32_t n) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) out[k] = a[k] + b[k];
+}
+
 // SELL-32 bond slab from the reference CSR, one warp per chunk of 32 nodes (lane = node): bond k of
 // node 32c + lane goes to slot chunk_slot[c] + 32k + lane with its global neighbour index and
 // xi_norm = |pos[j] - pos[i]| (gen_xi, particle2.h:236-252; the FP64 operations of the reference,
@@ -432,26 +442,24 @@ static int create_impl(const pg_setup_desc* s, const pg_config* cfg_in, pg_handl
   P.xpos = P.pos;
   CU(h->dalloc(&P.vol, N));
   CU(h->dalloc(&P.curf, (size_t)N * S));
-  pack(s->pos);
-  CU(cudaMemcpy(P.pos, tmp.data(), tmp.size() * 8, cudaMemcpyHostToDevice));
-  pack(s->disp);
-  CU(cudaMemcpy(P.disp, tmp.data(), tmp.size() * 8, cudaMemcpyHostToDevice));
-  {
-    // CurrPos before the first step is pos + disp (only used for the grid origin)
-    std::vector<double> cu(tmp.size());
-    for (size_t i = 0; i < tmp.size(); ++i) cu[i] = 0.0;
-    for (uint32_t i = 0; i < N; ++i)
-      for (uint32_t c = 0; c < D; ++c) cu[(size_t)i * S + c] = s->pos[(size_t)i * D + c] + s->disp[(size_t)i * D + c];
-    CU(cudaMemcpy(P.cur, cu.data(), cu.size() * 8, cudaMemcpyHostToDevice));
+  // in 2D the stride is the dimension: straight uploads; in 3D through the padded host buffer
+  auto upload = [&](double* dst, const double* src) -> cudaError_t {
+    if (S == D) return cudaMemcpy(dst, src, (size_t)N * D * 8, cudaMemcpyHostToDevice);
+    pack(src);
+    return cudaMemcpy(dst, tmp.data(), tmp.size() * 8, cudaMemcpyHostToDevice);
+  };
+  CU(upload(P.pos, s->pos));
+  CU(upload(P.disp, s->disp));
+  CU(upload(h->vel_a, s->vel));
+  CU(cudaMemcpy(h->vel_b, h->vel_a, (size_t)N * S * 8, cudaMemcpyDeviceToDevice));
+  CU(upload(P.acc, s->acc));
+  CU(upload(P.extf, s->extforce));
+  CU(cudaMemset(P.force, 0, (size_t)N * S * 8));
+  // CurrPos before the first step is pos + disp (only used for the grid origin)
+  if (N) {
+    k_add_vec<<<(N * S + 255) / 256, 256>>>(P.pos, P.disp, P.cur, N * S);
+    CU(cudaGetLastError());
   }
-  pack(s->vel);
-  CU(cudaMemcpy(h->vel_a, tmp.data(), tmp.size() * 8, cudaMemcpyHostToDevice));
-  CU(cudaMemcpy(h->vel_b, tmp.data(), tmp.size() * 8, cudaMemcpyHostToDevice));
-  pack(s->acc);
-  CU(cudaMemcpy(P.acc, tmp.data(), tmp.size() * 8, cudaMemcpyHostToDevice));
-  pack(s->extforce);
-  CU(cudaMemcpy(P.extf, tmp.data(), tmp.size() * 8, cudaMemcpyHostToDevice));
-  CU(cudaMemset(P.force, 0, tmp.size() * 8));
   CU(cudaMemcpy(P.vol, s->vol, (size_t)N * 8, cudaMemcpyHostToDevice));
   tr.mark("node vectors");
 
