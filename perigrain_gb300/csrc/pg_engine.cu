@@ -233,11 +233,17 @@ static int validate(const pg_setup_desc* s, const pg_config* c) {
   if (s->bond_offset[s->n_nodes] && !s->bond_local) return fail(PG_EINVAL, "missing bond_local");
   for (uint32_t g = 0; g < s->n_grains; ++g) {
     uint32_t n0 = s->grain_node_offset[g], n1 = s->grain_node_offset[g + 1];
-    for (uint32_t i = n0; i < n1; ++i) {
+    for (uint32_t i = n0; i < n1; ++i)
       if (s->bond_offset[i + 1] < s->bond_offset[i]) return fail(PG_EINVAL, "bond_offset decreasing");
-      for (uint64_t b = s->bond_offset[i]; b < s->bond_offset[i + 1]; ++b)
-        if (s->bond_local[b] >= n1 - n0)
-          return fail(PG_EINVAL, "bond of node " + std::to_string(i) + " points outside its grain");
+    // the grain's rows are one contiguous range: its largest local index decides (a branch-free
+    // reduction), the offending node is looked up only on failure
+    uint32_t mx = 0;
+    for (uint64_t b = s->bond_offset[n0]; b < s->bond_offset[n1]; ++b) mx = std::max(mx, s->bond_local[b]);
+    if (s->bond_offset[n1] > s->bond_offset[n0] && mx >= n1 - n0) {
+      for (uint32_t i = n0; i < n1; ++i)
+        for (uint64_t b = s->bond_offset[i]; b < s->bond_offset[i + 1]; ++b)
+          if (s->bond_local[b] >= n1 - n0)
+            return fail(PG_EINVAL, "bond of node " + std::to_string(i) + " points outside its grain");
     }
     for (uint32_t k = s->bdry_offset[g]; k < s->bdry_offset[g + 1]; ++k)
       if (s->bdry_nodes[k] >= n1 - n0) return fail(PG_EINVAL, "bdry node out of range");
