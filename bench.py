@@ -463,17 +463,23 @@ def main():
     # end to end through the C ABI from host buffers
     t0 = time.perf_counter()
     e2e_sim = Simulation(setup, **kw)
+    t_created = time.perf_counter()
     snaps = 0
     done = 0
     d2h = 0
+    t_dl = 0.0
     while done < a.steps:
         n = min(100, a.steps - done)
         e2e_sim.step(n)
         done += n
+        td = time.perf_counter()
         for f in ("CurrPos", "vel", "acc", "force"):
             d2h += e2e_sim.field(f).nbytes
+        t_dl += time.perf_counter() - td
         snaps += 1
     e2e_s = time.perf_counter() - t0
+    e2e_parts = {"create_ms": (t_created - t0) * 1e3, "download_ms": t_dl * 1e3,
+                 "steps_ms": (e2e_s - (t_created - t0) - t_dl) * 1e3}
     e2e_sim.close()
     h2d = sum(getattr(setup, f).nbytes for f in ("pos", "vol", "disp", "vel", "acc", "extforce", "bond_offset",
                                                    "bond_local"))
@@ -511,7 +517,8 @@ def main():
                                                cpu_info["nodes"], cpu_info["seconds"])},
         "e2e": {"value": setup.n_nodes * a.steps / e2e_s, "unit": METRIC,
                 "h2d_bytes_per_step": h2d / a.steps, "d2h_bytes_per_step": d2h / a.steps,
-                "note": "pg_create from host arrays + %d steps + %d tc_ snapshot downloads" % (a.steps, snaps)},
+                "note": "pg_create from host arrays + %d steps + %d tc_ snapshot downloads" % (a.steps, snaps),
+                **e2e_parts},
         "gpu_launches": launches,
         "clocks": clk.summary(),
         "autotuned": tuned,

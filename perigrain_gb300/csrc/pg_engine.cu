@@ -330,6 +330,12 @@ int pg_create(const pg_setup_desc* s, const pg_config* cfg_in, pg_handle** out) 
   return create_impl(s, &c, out);
 }
 
+// out[i][c] = (double)f[i * S + c], c < D
+__global__ void k_widen_field(const float* f, uint32_t S, uint32_t D, uint32_t N, double* out) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < N * D) out[k] = (double)f[(size_t)(k / D) * S + k % D];
+}
+
 // out[k] = a[k] + b[k]
 __global__ void k_add_vec(const double* a, const double* b, double* out, uint32_t n) {
   const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -846,17 +852,25 @@ int pg_get_field(pg_handle* h, int field, double* out) {
   if (rc) return rc;
   const uint32_t N = h->P.N, D = h->dim, S = h->S;
   if (h->precision == PG_MIXED && (field == PG_FIELD_ACC || field == PG_FIELD_FORCE)) {
-    std::vector<float> tf((size_t)N * S);
-    CU(cudaMemcpy(tf.data(), field == PG_FIELD_ACC ? h->P.acc_f : h->P.force_f, tf.size() * 4,
-                  cudaMemcpyDeviceToHost));
-    for (uint32_t i = 0; i < N; ++i)
-      for (uint32_t c = 0; c < D; ++c) out[(size_t)i * D + c] = (double)tf[(size_t)i * S + c];
+    // the FP32 field widened on the device into [N][D] doubles, then one copy
+    if (!h->field_scratch) CU(h->dalloc(&h->field_scratch, (size_t)N * D));
+    if (N) {
+      k_widen_field<<<(N * D + 255) / 256, 256, 0, h->stream>>>(
+          field == PG_FIELD_ACC ? h->P.acc_f : h->P.force_f, S, D, N, h->field_scratch);
+      CU(cudaGetLastError());
+      CU(cudaMemcpyAsync(out, h->field_scratch, (size_t)N * D * 8, cudaMemcpyDeviceToHost, h->stream));
+      CU(cudaStreamSynchronize(h->stream));
+    }
     return PG_OK;
   }
-  std::vector<double> tmp((size_t)N * S);
-  CU(cudaMemcpy(tmp.data(), src, tmp.size() * 8, cudaMemcpyDeviceToHost));
-  for (uint32_t i = 0; i < N; ++i)
-    for (uint32_t c = 0; c < D; ++c) out[(size_t)i * D + c] = tmp[(size_t)i * S + c];
+  if (S == D) {
+    CU(cudaMemcpy(out, src, (size_t)N * D * 8, cudaMemcpyDeviceToHost));
+  } else {
+    std::vector<double> tmp((size_t)N * S);
+    CU(cudaMemcpy(tmp.data(), src, tmp.size() * 8, cudaMemcpyDeviceToHost));
+    for (uint32_t i = 0; i < N; ++i)
+      for (uint32_t c = 0; c < D; ++c) out[(size_t)i * D + c] = tmp[(size_t)i * S + c];
+  }
   if (field == PG_FIELD_DISP) {
     std::vector<uint8_t> pend(N);
     CU(cudaMemcpy(pend.data(), h->P.clamp_pending, N, cudaMemcpyDeviceToHost));

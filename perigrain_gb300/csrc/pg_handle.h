@@ -148,6 +148,7 @@ struct pg_handle {
   // post-processing scratch (pg_postprocess)
   double* post_sum = nullptr;
   double* post_damage = nullptr;
+  double* field_scratch = nullptr;  // [N][D] doubles: FP32 fields widened for pg_get_field
 
   ~pg_handle() {
     if (stream) cudaStreamSynchronize(stream);
