@@ -195,7 +195,9 @@ __global__ void __launch_bounds__(128) k_force(const Dev P) {
   if (act) ldv<D>(P.cur, d, xpc);
 
   // ---- node-node contact: self-contact first, then grains j ascending (timeloop.h:709-747) ----
-  if ((selfc || other) && p_bdry) {
+  // with candidate lists a node whose list is empty has no contact this step
+  const uint32_t ncl = (P.cand_q && act) ? (uint32_t)P.cand_n[d] : 0u;
+  if ((selfc || other) && p_bdry && (!P.cand_q || ncl > 0)) {
     double bmn[D], bmx[D];
     grain_box<D>(P, g, bmn, bmx);
     float pf[D];
@@ -233,7 +235,6 @@ __global__ void __launch_bounds__(128) k_force(const Dev P) {
     };
     if (P.cand_q) {
       // candidate list of the last rebuild (a superset of the grid search's candidates)
-      const uint32_t ncl = P.cand_n[d];
       const size_t cbase = (size_t)chunk * P.cand_cap * 32 + lane;
       for (uint32_t k = 0; k < ncl; ++k) consider(P.cand_q[cbase + (size_t)k * 32]);
     } else {

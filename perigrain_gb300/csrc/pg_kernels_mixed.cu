@@ -414,7 +414,9 @@ __global__ void __launch_bounds__(128) k_force_mx(const Dev P) {
   float vp[D];
   for (int c = 0; c < D; ++c) vp[c] = act ? (float)vpd[c] : 0.f;
 
-  if ((selfc || other) && p_bdry) {
+  // with candidate lists a node whose list is empty has no contact this step
+  const uint32_t ncl = (P.cand_q && act) ? (uint32_t)P.cand_n[d] : 0u;
+  if ((selfc || other) && p_bdry && (!P.cand_q || ncl > 0)) {
     double bmn[D], bmx[D];
     grain_box<D>(P, g, bmn, bmx);
     float ph[D], pl[D];
@@ -452,7 +454,6 @@ __global__ void __launch_bounds__(128) k_force_mx(const Dev P) {
     };
     if (P.cand_q) {
       // candidate list of the last rebuild (a superset of the grid search's candidates)
-      const uint32_t ncl = P.cand_n[d];
       const size_t cbase = (size_t)chunk * P.cand_cap * 32 + lane;
       uint32_t qn = ncl ? P.cand_q[cbase] : d;  // the next entry is loaded one candidate ahead
       for (uint32_t k = 0; k < ncl; ++k) {
