@@ -202,7 +202,10 @@ void pg_config_default(pg_config* c) {
   c->contact_skin = 0.25;
 }
 
-static int validate(const pg_setup_desc* s, const pg_config* c) {
+// Host validation of a setup. With bonds_on_host the bond rows are checked here too (offsets
+// non-decreasing, neighbours inside their grain); otherwise k_check_bonds checks them on the
+// device from the uploaded copy before anything reads through them.
+static int validate(const pg_setup_desc* s, const pg_config* c, bool bonds_on_host) {
   if (!s || !c) return fail(PG_EINVAL, "null setup or config");
   if (!(c->contact_skin >= 0) || !std::isfinite(c->contact_skin)) return fail(PG_EINVAL, "contact_skin must be >= 0");
   if (s->dim != 2 && s->dim != 3) return fail(PG_EINVAL, "dim must be 2 or 3");
@@ -233,17 +236,19 @@ static int validate(const pg_setup_desc* s, const pg_config* c) {
   if (s->bond_offset[s->n_nodes] && !s->bond_local) return fail(PG_EINVAL, "missing bond_local");
   for (uint32_t g = 0; g < s->n_grains; ++g) {
     uint32_t n0 = s->grain_node_offset[g], n1 = s->grain_node_offset[g + 1];
-    for (uint32_t i = n0; i < n1; ++i)
-      if (s->bond_offset[i + 1] < s->bond_offset[i]) return fail(PG_EINVAL, "bond_offset decreasing");
-    // the grain's rows are one contiguous range: its largest local index decides (a branch-free
-    // reduction), the offending node is looked up only on failure
-    uint32_t mx = 0;
-    for (uint64_t b = s->bond_offset[n0]; b < s->bond_offset[n1]; ++b) mx = std::max(mx, s->bond_local[b]);
-    if (s->bond_offset[n1] > s->bond_offset[n0] && mx >= n1 - n0) {
+    if (bonds_on_host) {
       for (uint32_t i = n0; i < n1; ++i)
-        for (uint64_t b = s->bond_offset[i]; b < s->bond_offset[i + 1]; ++b)
-          if (s->bond_local[b] >= n1 - n0)
-            return fail(PG_EINVAL, "bond of node " + std::to_string(i) + " points outside its grain");
+        if (s->bond_offset[i + 1] < s->bond_offset[i]) return fail(PG_EINVAL, "bond_offset decreasing");
+      // the grain's rows are one contiguous range: its largest local index decides, the offending
+      // node is looked up only on failure
+      uint32_t mx = 0;
+      for (uint64_t b = s->bond_offset[n0]; b < s->bond_offset[n1]; ++b) mx = std::max(mx, s->bond_local[b]);
+      if (s->bond_offset[n1] > s->bond_offset[n0] && mx >= n1 - n0) {
+        for (uint32_t i = n0; i < n1; ++i)
+          for (uint64_t b = s->bond_offset[i]; b < s->bond_offset[i + 1]; ++b)
+            if (s->bond_local[b] >= n1 - n0)
+              return fail(PG_EINVAL, "bond of node " + std::to_string(i) + " points outside its grain");
+      }
     }
     for (uint32_t k = s->bdry_offset[g]; k < s->bdry_offset[g + 1]; ++k)
       if (s->bdry_nodes[k] >= n1 - n0) return fail(PG_EINVAL, "bdry node out of range");
@@ -342,6 +347,27 @@ __global__ void k_add_vec(const double* a, const double* b, double* out, uint32_
   if (k < n) out[k] = a[k] + b[k];
 }
 
+// Bond rows of the uploaded CSR: offsets non-decreasing (and within the nb bonds), every neighbour
+// inside its node's grain. The smallest (kind << 32 | node) found goes to *bad, kind 0 = offsets,
+// 1 = neighbour; *bad stays ~0 for a valid setup.
+__global__ void k_check_bonds(const uint64_t* off, const uint32_t* loc, const uint32_t* grain_node_offset,
+                              const uint32_t* node_grain, uint32_t N, uint64_t nb, unsigned long long* bad) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  const uint64_t lo = off[i], hi = off[i + 1];
+  if (hi < lo || hi > nb) {
+    atomicMin(bad, (unsigned long long)i);
+    return;
+  }
+  const uint32_t g = node_grain[i];
+  const uint32_t n = grain_node_offset[g + 1] - grain_node_offset[g];
+  for (uint64_t b = lo; b < hi; ++b)
+    if (loc[b] >= n) {
+      atomicMin(bad, (1ull << 32) | i);
+      return;
+    }
+}
+
 // SELL-32 bond slab from the reference CSR, one warp per chunk of 32 nodes (lane = node): bond k of
 // node 32c + lane goes to slot chunk_slot[c] + 32k + lane with its global neighbour index and
 // xi_norm = |pos[j] - pos[i]| (gen_xi, particle2.h:236-252; the FP64 operations of the reference,
@@ -393,11 +419,14 @@ static int create_impl(const pg_setup_desc* s, const pg_config* cfg_in, pg_handl
   *out = nullptr;
   CreateTrace tr;
   pg_config cfg = *cfg_in;
-  int rc = validate(s, &cfg);
+  int ndev = 0;
+  const bool have_dev = cudaGetDeviceCount(&ndev) == cudaSuccess && ndev > 0;
+  // without a device everything is checked here (and the call ends with PG_ENODEV); with one the
+  // bond rows are checked by the device on their uploaded copy
+  int rc = validate(s, &cfg, !have_dev);
   if (rc) return rc;
   tr.mark("validate");
-  int ndev = 0;
-  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(PG_ENODEV, "no CUDA device");
+  if (!have_dev) return fail(PG_ENODEV, "no CUDA device");
   if (cfg.pair_log_capacity == 0) cfg.pair_log_capacity = 1024;
   if (cfg.max_contacts == 0) cfg.max_contacts = 48;
   if (cfg.max_contacts > (uint32_t)MAX_CAND) cfg.max_contacts = MAX_CAND;
@@ -505,6 +534,7 @@ static int create_impl(const pg_setup_desc* s, const pg_config* cfg_in, pg_handl
   h->chunk_word.resize(NC + 1);
   std::vector<uint32_t> chunk_deg(NC, 0);
   for (uint32_t i = 0; i < N; ++i) {
+    if (s->bond_offset[i + 1] < s->bond_offset[i]) return fail(PG_EINVAL, "bond_offset decreasing");
     h->node_deg[i] = (uint32_t)(s->bond_offset[i + 1] - s->bond_offset[i]);
     chunk_deg[i >> 5] = std::max<uint32_t>(chunk_deg[i >> 5], h->node_deg[i]);
   }
@@ -543,6 +573,24 @@ static int create_impl(const pg_setup_desc* s, const pg_config* cfg_in, pg_handl
     if (e == cudaSuccess) e = cudaMemcpy(d_off, s->bond_offset, (size_t)(N + 1) * 8, cudaMemcpyHostToDevice);
     if (e == cudaSuccess && nb) e = cudaMemcpy(d_loc, s->bond_local, (size_t)nb * 4, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(d_gno, s->grain_node_offset, (size_t)(G + 1) * 4, cudaMemcpyHostToDevice);
+    // bond rows checked before anything reads through them
+    unsigned long long bad = ~0ull, *d_bad = nullptr;
+    if (e == cudaSuccess) e = cudaMalloc((void**)&d_bad, 8);
+    if (e == cudaSuccess) e = cudaMemcpy(d_bad, &bad, 8, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+      k_check_bonds<<<(N + 255) / 256, 256>>>(d_off, d_loc, d_gno, P.node_grain, N, nb, d_bad);
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(&bad, d_bad, 8, cudaMemcpyDeviceToHost);
+    if (d_bad) cudaFree(d_bad);
+    if (e == cudaSuccess && bad != ~0ull) {
+      cudaFree(d_off);
+      cudaFree(d_loc);
+      cudaFree(d_gno);
+      const uint32_t node = (uint32_t)(bad & 0xffffffffu);
+      if ((bad >> 32) == 0) return fail(PG_EINVAL, "bond_offset decreasing");
+      return fail(PG_EINVAL, "bond of node " + std::to_string(node) + " points outside its grain");
+    }
     if (e == cudaSuccess) {
       k_layout_bonds<<<NC, 32>>>(P.pos, S, D, N, d_off, d_loc, d_gno, P.node_grain, P.chunk_slot, P.chunk_word,
                                  P.chunk_deg, P.bcol, P.bxin, P.alive);
