@@ -435,7 +435,7 @@ static __global__ void __launch_bounds__(FINAL_THREADS) k_finalize(const Dev P) 
   const uint32_t nrx = P.I * NS * D;
   for (uint32_t i = tid; i < nrx; i += blockDim.x) P.reaction[i] = 0.0;
   if (R > 0) {
-    if (R > (uint32_t)WREC_SMEM_CAP || R > P.wrec_cap) {
+    if (R > P.wrec_smem || R > P.wrec_cap) {
       if (tid == 0) set_status(P.status, PG_ECAPACITY);
     } else {
       // sort the records by (side, node in the reference's loop order); the index of the record

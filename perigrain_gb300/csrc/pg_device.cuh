@@ -155,6 +155,7 @@ struct Dev {
   WallRec* wrec;
   uint32_t* wrec_count;
   uint32_t wrec_cap;
+  uint32_t wrec_smem;  // wall records the finalize launch's shared memory holds (0 without walls)
   // pair log
   unsigned long long* pair_acc;  // [2]: count, hash
   unsigned long long *log_count, *log_hash;

@@ -732,6 +732,12 @@ static int create_impl(const pg_setup_desc* s, const pg_config* cfg_in, pg_handl
 
   // ---- wall records, logs, control ----
   P.wrec_cap = (uint32_t)std::min<uint64_t>(WREC_SMEM_CAP, 2ull * D * N);
+  {
+    // the finalize kernel takes its large shared-memory buffer only when walls can make records
+    bool any_wall = false;
+    for (uint32_t k = 0; k < I; ++k) any_wall = any_wall || h->inst_host[k].allow_wall;
+    P.wrec_smem = any_wall ? (uint32_t)WREC_SMEM_CAP : 0u;
+  }
   CU(h->dalloc(&P.wrec, P.wrec_cap));
   CU(h->dalloc(&P.wrec_count, 1));
   CU(cudaMemset(P.wrec_count, 0, 4));

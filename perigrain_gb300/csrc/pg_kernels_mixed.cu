@@ -768,7 +768,7 @@ static void launch_mx(const Dev& P, const LaunchCfg& L, cudaStream_t s, uint64_t
     else launch_k(k_force_mx<D, false, false>, grid, block, 0, s, pdl, P);
   }
   if (e1) cudaEventRecord(e1, s);
-  launch_k(k_finalize<D>, finalize_blocks(P.I), FINAL_THREADS, FINAL_SMEM, s, pdl, P);
+  launch_k(k_finalize<D>, finalize_blocks(P.I), FINAL_THREADS, P.wrec_smem ? FINAL_SMEM : 0, s, pdl, P);
   *launches += 2;
 }
 
