@@ -325,6 +325,18 @@ __global__ void __launch_bounds__(128) k_force_mx(const Dev P) {
   for (int c = 0; c < D; ++c) f[c] = 0.f;
   double vpd[D];
   if (act) ldv<D>(P.vel_in, d, vpd);
+  // per-node inputs of the epilogue: in 2D loaded up front so their latency hides behind the bond
+  // loop; in 3D where they are used (the extra live registers spill there and measured slower)
+  constexpr int DE = (D == 2) ? D : 1;
+  float ef_in[DE], ao_in[DE];
+  bool clamped_in = false;
+  if constexpr (D == 2) {
+    if (mov) {
+      ldvf<D>(P.extf_f, d, ef_in);
+      ldvf<D>(P.acc_f, d, ao_in);
+      clamped_in = P.clamped[d] != 0;
+    }
+  }
 
   const bool brk = P.enable_fracture && (gr.flags & GF_BREAKABLE) && (gr.flags & GF_BREAK_BONDS);
   const float cnot = (float)gr.cnot, snot = (float)gr.snot;
@@ -663,12 +675,20 @@ __global__ void __launch_bounds__(128) k_force_mx(const Dev P) {
 
   if (mov && P.worm) {
     float ef[D];
-    ldvf<D>(P.extf_f, d, ef);
+    if constexpr (D == 2) {
+      for (int c = 0; c < D; ++c) ef[c] = ef_in[c];
+    } else {
+      ldvf<D>(P.extf_f, d, ef);
+    }
     const float gate = (float)((worm_phase(t) + 1u) % 2u);
     for (int c = 0; c < D; ++c) f[c] = fmaf(gate, ef[c], f[c]);
   } else if (mov) {
     float ef[D];
-    ldvf<D>(P.extf_f, d, ef);
+    if constexpr (D == 2) {
+      for (int c = 0; c < D; ++c) ef[c] = ef_in[c];
+    } else {
+      ldvf<D>(P.extf_f, d, ef);
+    }
     float sc = 1.f;
     if (P.gradient_extforce) {
       double scd = (double)t / (double)P.extforce_maxstep;
@@ -698,13 +718,17 @@ __global__ void __launch_bounds__(128) k_force_mx(const Dev P) {
     if (mov) {
       float ao[D], a[D];
       double v[D];
-      ldvf<D>(P.acc_f, d, ao);
+      if constexpr (D == 2) {
+        for (int c = 0; c < D; ++c) ao[c] = ao_in[c];
+      } else {
+        ldvf<D>(P.acc_f, d, ao);
+      }
       const float orho = (float)gr.one_over_rho, hdt = P.half_dt_f;
       for (int c = 0; c < D; ++c) {
         a[c] = orho * f[c];
         v[c] = vpd[c] + widen((ao[c] + a[c]) * hdt);  // FP64 accumulation of an FP32 increment
       }
-      if (P.clamped[d]) {
+      if ((D == 2) ? clamped_in : (P.clamped[d] != 0)) {
         for (int c = 0; c < D; ++c) {
           a[c] = 0.f;
           v[c] = 0.0;
