@@ -55,7 +55,17 @@ struct GrainDev {
   // grains contacts with the arithmetic mean of the two grains' values, which is the reference's
   // global parameter when all grains carry the same value.
   double kn, zeta, mu;
+  // FP32 copies of cnot, snot and 1/rho for the mixed kernels (set by set_grain_f whenever the
+  // FP64 values change; an FP64 -> FP32 conversion per thread would run on the FP64 pipe)
+  float cnot_f, snot_f, one_over_rho_f, pad_f;
 };
+
+inline void set_grain_f(GrainDev& g) {
+  g.cnot_f = (float)g.cnot;
+  g.snot_f = (float)g.snot;
+  g.one_over_rho_f = (float)g.one_over_rho;
+  g.pad_f = 0.f;
+}
 
 struct InstDev {
   double contact_rad, normal_stiffness, friction_coefficient, damping_ratio;

@@ -625,6 +625,7 @@ static int create_impl(const pg_setup_desc* s, const pg_config* cfg_in, pg_handl
     gd.kn = s->normal_stiffness[s->grain_instance[g]];
     gd.zeta = s->damping_ratio[s->grain_instance[g]];
     gd.mu = s->friction_coefficient[s->grain_instance[g]];
+    set_grain_f(gd);
   }
   CU(h->dalloc(&P.grain, G));
   CU(cudaMemcpy(P.grain, grains.data(), G * sizeof(GrainDev), cudaMemcpyHostToDevice));

@@ -310,6 +310,7 @@ int pg_set_grain_params(pg_handle* h, const double* cnot, const double* snot, co
     if (kn) g[k].kn = kn[k];
     if (zeta) g[k].zeta = zeta[k];
     if (mu) g[k].mu = mu[k];
+    set_grain_f(g[k]);
   }
   CU(cudaMemcpy(h->P.grain, g.data(), g.size() * sizeof(GrainDev), cudaMemcpyHostToDevice));
   if ((kn || zeta || mu) && !h->P.grain_contact) {

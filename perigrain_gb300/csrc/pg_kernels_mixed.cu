@@ -339,7 +339,7 @@ __global__ void __launch_bounds__(128) k_force_mx(const Dev P) {
   }
 
   const bool brk = P.enable_fracture && (gr.flags & GF_BREAKABLE) && (gr.flags & GF_BREAK_BONDS);
-  const float cnot = (float)gr.cnot, snot = (float)gr.snot;
+  const float cnot = gr.cnot_f, snot = gr.snot_f;
   const uint32_t cdeg = P.chunk_deg[chunk];
   const uint32_t slot0 = P.chunk_slot[chunk] + lane;
   const uint32_t w0 = P.chunk_word[chunk];
@@ -423,8 +423,6 @@ __global__ void __launch_bounds__(128) k_force_mx(const Dev P) {
   const bool p_bdry = !P.nl_bdry_only || (act && P.bdry_rank[d] != NONE);
   const bool selfc = mov && P.enable_fracture && (gr.flags & GF_BREAKABLE) && P.self_contact;
   const bool other = mov && (P.worm || (gr.flags & GF_STOPPABLE));
-  float vp[D];
-  for (int c = 0; c < D; ++c) vp[c] = act ? (float)vpd[c] : 0.f;
 
   // with candidate lists a node whose list is empty has no contact this step
   const uint32_t ncl = (P.cand_q && act) ? (uint32_t)P.cand_n[d] : 0u;
@@ -622,7 +620,7 @@ __global__ void __launch_bounds__(128) k_force_mx(const Dev P) {
         rec.has_fric = 0;
         rec.has_damp = 0;
         float rv[D];
-        for (int c = 0; c < D; ++c) rv[c] = vp[c];
+        for (int c = 0; c < D; ++c) rv[c] = (float)vpd[c];
         rv[dir] -= (float)in.wall_speed[side];
         if (P.allow_friction) {
           if constexpr (D == 2) {
@@ -723,7 +721,7 @@ __global__ void __launch_bounds__(128) k_force_mx(const Dev P) {
       } else {
         ldvf<D>(P.acc_f, d, ao);
       }
-      const float orho = (float)gr.one_over_rho, hdt = P.half_dt_f;
+      const float orho = gr.one_over_rho_f, hdt = P.half_dt_f;
       for (int c = 0; c < D; ++c) {
         a[c] = orho * f[c];
         v[c] = vpd[c] + widen((ao[c] + a[c]) * hdt);  // FP64 accumulation of an FP32 increment
