@@ -241,7 +241,8 @@ __global__ void __launch_bounds__(256) k_predict_mx(const Dev P) {
       // 0.45 skin since the last build
       float m2 = 0.f;
       for (int c = 0; c < D; ++c) {
-        const float dd = (float)dp[c] - db[c];
+        double dpt;
+        const float dd = trunc_f32(dp[c], &dpt) - db[c];  // truncation (integer ops), not an FP64 conversion
         m2 += dd * dd;
       }
       if (m2 > in.skin_lim2) *P.rebuild = 1;
