@@ -55,11 +55,35 @@ __device__ __forceinline__ double widen(float f) {
   const unsigned long long ee = (e == 0xff) ? 0x7ffull : (unsigned long long)(e + 896);
   return __longlong_as_double((long long)(sgn | (ee << 52) | ((unsigned long long)(b & 0x7fffffu) << 29)));
 }
-// hi/lo pair: x = hi + lo + O(2^-47 |x|)
+// hi/lo pair: x = hi + lo + O(2^-47 |x|); hi = trunc_f32(x), lo = trunc_f32(x - hi). When hi is an
+// FP32 normal number the difference x - hi is exactly x's low 29 mantissa bits, so lo is formed
+// from them with integer instructions (identical bits, no FP64 subtraction); otherwise the FP64
+// route.
 __device__ __forceinline__ void split_hl(double x, float* hi, float* lo) {
-  double hd, ld;
-  *hi = trunc_f32(x, &hd);
-  *lo = trunc_f32(x - hd, &ld);
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned int hw = (unsigned int)(b >> 32);
+  const int e = (int)((hw >> 20) & 0x7ffu);
+  if (e < 1023 - 126 || e > 1023 + 127) {
+    double hd, ld;
+    *hi = trunc_f32(x, &hd);
+    *lo = trunc_f32(x - hd, &ld);
+    return;
+  }
+  const unsigned int sgn = hw & 0x80000000u;
+  *hi = __uint_as_float(sgn | ((unsigned int)(e - 896) << 23) | (unsigned int)((b >> 29) & 0x7fffffu));
+  const unsigned int r = (unsigned int)(b & ((1ull << 29) - 1));
+  if (r == 0) {  // x - hi = +0
+    *lo = 0.0f;
+    return;
+  }
+  const int p = 31 - __clz(r);  // leading bit of the remainder
+  const int ed = e + p - 52;     // biased FP64 exponent of x - hi
+  if (ed < 1023 - 126) {         // below the FP32 normal range: signed zero
+    *lo = __uint_as_float(sgn);
+    return;
+  }
+  const unsigned int frac = (p <= 23) ? ((r << (23 - p)) & 0x7fffffu) : ((r >> (p - 23)) & 0x7fffffu);
+  *lo = __uint_as_float(sgn | ((unsigned int)(ed - 896) << 23) | frac);
 }
 
 template <int D>
