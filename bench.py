@@ -252,6 +252,99 @@ def adjoint_bench(n_steps=5000, checkpoint_every=100, n_fd=4):
                     "their gradients) separate and h=1e-4 differences are nonlinear"}
 
 
+def bonds_bench(n_target=200_000, repeats=5):
+    """GPU bond-list builder (pg_build_bonds) on one jittered 2D disk grain of ~200k nodes with the
+    horizon delta = 3h: grain nodes per second with positions resident on the device, end to end
+    from a host array, and the reference's algorithm (all n(n-1)/2 pairs through
+    itertools.combinations, exp_dict.py:199-222) in Python on a 1,200-node grain. The reference's
+    cost grows with n^2, so its rate on the large grain would be far lower still."""
+    import itertools
+    import math
+
+    import ctypes as C
+    import torch
+
+    from perigrain_gb300 import _native as N
+    from perigrain_gb300 import bonds, setups
+
+    h = 1e-5
+    rng = np.random.default_rng(5)
+    p, _ = setups.grid_nodes("disk", h * math.sqrt(n_target / math.pi), h, 2, 6, 0.1, rng, 0.0)
+    p = np.ascontiguousarray(p, np.float64)
+    delta = 3 * h
+    n = len(p)
+    d_pos = torch.from_numpy(p).cuda()
+    cap = n * 32
+    d_pairs = torch.empty((cap, 2), dtype=torch.int32, device="cuda")
+    npairs = C.c_uint64()
+    L = N.lib()
+
+    def build():
+        N.check(L.pg_build_bonds(C.c_void_p(d_pos.data_ptr()), n, 2, delta, C.c_void_p(d_pairs.data_ptr()), cap,
+                                 C.byref(npairs), None))
+
+    build()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(repeats):
+        build()
+    dev_s = (time.perf_counter() - t0) / repeats
+    t0 = time.perf_counter()
+    pairs = bonds.build_bonds(p, delta, capacity=cap)
+    e2e_s = time.perf_counter() - t0
+    # the reference's rule on a small grain, in Python
+    ps, _ = setups.grid_nodes("disk", h * math.sqrt(1200 / math.pi), h, 2, 6, 0.1, np.random.default_rng(6), 0.0)
+    ps = [tuple(map(float, q)) for q in ps]
+    t0 = time.perf_counter()
+    found = 0
+    for a, b in itertools.combinations(range(len(ps)), 2):
+        if math.sqrt((ps[b][0] - ps[a][0]) ** 2 + (ps[b][1] - ps[a][1]) ** 2) <= delta:
+            found += 1
+    cpu_s = time.perf_counter() - t0
+    return {"workload": "one 2D disk grain, %d nodes, delta = 3h, %d bonds" % (n, len(pairs)),
+            "metric": "grain nodes/s", "value": n / dev_s, "ms": dev_s * 1e3, "bonds": int(npairs.value),
+            "e2e": {"value": n / e2e_s, "unit": "grain nodes/s", "note": "host positions -> device, build, pairs -> host"},
+            "cpu_baseline": {"value": len(ps) / cpu_s, "unit": "grain nodes/s", "cores": 1, "kind": "port",
+                             "sample": "the reference's all-pairs rule in Python on a %d-node grain (%d bonds), %.2f s"
+                                       % (len(ps), found, cpu_s)}}
+
+
+def postprocess_bench(sim, setup, repeats=20):
+    """On-device post-processing (pg_postprocess) of the workload's state: snapshots per second,
+    against the reference scripts' numpy formulas (read_sim_output.py) applied on the host to
+    the same fields already in host memory (file reading excluded)."""
+    sim.synchronize()
+    sim.postprocess()
+    t0 = time.perf_counter()
+    for _ in range(repeats):
+        sim.postprocess(node_damage=True)
+    dev_s = (time.perf_counter() - t0) / repeats
+    fields = {f: sim.field(f) for f in ("vel", "acc", "CurrPos", "force")}
+    alive = sim.bond_alive()
+    off = np.asarray(setup.grain_node_offset, np.int64)
+    vol = np.asarray(setup.vol, np.float64)
+    rho = np.asarray(setup.rho, np.float64)
+    t0 = time.perf_counter()
+    deg0 = np.diff(setup.bond_offset.astype(np.int64)).astype(np.float64)
+    row = np.repeat(np.arange(setup.n_nodes), np.diff(setup.bond_offset.astype(np.int64)))
+    deg = np.bincount(row, weights=alive.astype(np.float64), minlength=setup.n_nodes)
+    dmg = (deg0 - deg) / deg0
+    for g in range(setup.n_grains):
+        sl = slice(off[g], off[g + 1])
+        fields["vel"][sl].mean(axis=0)
+        fields["acc"][sl].mean(axis=0)
+        fields["CurrPos"][sl].mean(axis=0)
+        fields["force"][sl].sum(axis=0)
+        np.mean(dmg[sl])
+        np.sum((vol[sl] * rho[g])[:, None] * fields["acc"][sl], axis=0)
+    cpu_s = time.perf_counter() - t0
+    return {"workload": "state of the bench workload, %d nodes, %d grains" % (setup.n_nodes, setup.n_grains),
+            "metric": "snapshots/s", "value": 1.0 / dev_s, "ms": dev_s * 1e3,
+            "cpu_baseline": {"value": 1.0 / cpu_s, "unit": "snapshots/s", "cores": 1, "kind": "port",
+                             "sample": "numpy formulas of read_sim_output.py on the same state in host memory, %.3f s"
+                                       % cpu_s}}
+
+
 def packing_bench(nx=800, ny=500, repeats=3):
     """Incircle packing (pg_pack_incenters) of a jittered 800 x 500-cell triangulated rectangle with
     the reference's default options (maximin nodal circles, boundary nodes included): circles per
@@ -302,7 +395,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=400)
     ap.add_argument("--no-adjoint", action="store_true", help="skip the gradient-path measurement")
-    ap.add_argument("--no-packing", action="store_true", help="skip the packing-generator measurement")
+    ap.add_argument("--no-packing", action="store_true",
+                    help="skip the setup-side measurements (packing generator, bond builder, post-processing)")
     ap.add_argument("--profile-adjoint", type=int, default=0, metavar="STEPS",
                     help="only a forward + backward of STEPS steps of the differentiable compaction "
                          "(checkpoint every 100; the command profiled under ncu)")
@@ -416,6 +510,7 @@ def main():
         raise RuntimeError("device status %d after the timed region" % st)
     total_steps = a.warmup + 2 * a.steps
     x_main = sim.field("CurrPos")
+    post_line = None if (a.no_packing or rank != 0) else postprocess_bench(sim, setup)
     sim.close()
 
     plain = seq = accuracy = None
@@ -496,6 +591,7 @@ def main():
     cpu_v, cpu_info = cpu_reference(setup, spec, a.cpu_steps, threads)
     adjoint = None if a.no_adjoint else adjoint_bench()
     packing_line = None if a.no_packing else packing_bench()
+    bonds_line = None if a.no_packing else bonds_bench()
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": ms_max / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -527,6 +623,8 @@ def main():
         "accuracy": accuracy,
         "adjoint": adjoint,
         "packing": packing_line,
+        "bond_builder": bonds_line,
+        "postprocess": post_line,
     }
     print(json.dumps(line), flush=True)
     if dist:
