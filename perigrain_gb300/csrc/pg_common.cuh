@@ -538,6 +538,7 @@ static __global__ void __launch_bounds__(FINAL_THREADS) k_finalize(const Dev P) 
 
 
 inline uint32_t cdiv(uint32_t a, uint32_t b) { return (a + b - 1) / b; }
+__device__ __forceinline__ uint32_t cdiv_dev(uint32_t a, uint32_t b) { return (a + b - 1) / b; }
 
 // ---------------------------------------------------------------------------------------------
 // Contact candidate lists (Verlet lists with a skin): on rebuild steps the grid is recounted and
@@ -639,12 +640,144 @@ static __global__ void __launch_bounds__(128) k_cand_build(const Dev P) {
   P.cand_n[d] = (uint8_t)n;
 }
 
+// ---------------------------------------------------------------------------------------------
+// Cooperative grid build (candidate lists): keys and counts, scan of the counts and scatter in one
+// launch of co-resident blocks separated by grid barriers, so a step without a rebuild costs one
+// idle launch here instead of four. The barrier waits are bounded: past GBAR_SPIN_LIMIT polls a
+// block records PG_ETIMEOUT and returns (the step's status then reports it).
+// ---------------------------------------------------------------------------------------------
+constexpr uint32_t GBAR_SPIN_LIMIT = 1u << 22;  // polls of ~64 ns: about 0.3 s
+
+__device__ __forceinline__ bool grid_barrier(const Dev& P, uint32_t* ok_smem) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t ok = 1;
+    volatile uint32_t* gen = P.gbar + 1;
+    const uint32_t g = *gen;
+    __threadfence();
+    if (atomicAdd(P.gbar, 1u) == gridDim.x - 1) {
+      atomicExch(P.gbar, 0u);
+      __threadfence();
+      atomicAdd(P.gbar + 1, 1u);
+    } else {
+      uint32_t it = 0;
+      while (*gen == g) {
+        if (++it > GBAR_SPIN_LIMIT) {
+          ok = 0;
+          set_status(P.status, PG_ETIMEOUT);
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+    *ok_smem = ok;
+  }
+  __syncthreads();
+  return *ok_smem != 0;
+}
+
+template <int D>
+static __global__ void __launch_bounds__(SCAN_THREADS) k_grid_coop(const Dev P) {
+  pdl_enter();
+  __shared__ uint32_t ws[32];
+  __shared__ uint32_t ok;
+  __shared__ bool last;
+  if (!*P.rebuild) return;  // set by the predict kernel before this launch: the same for every block
+  const uint32_t nthr = gridDim.x * blockDim.x;
+  // 1. grid keys and per-cell ranks
+  for (uint32_t d = blockIdx.x * blockDim.x + threadIdx.x; d < P.N; d += nthr) {
+    const InstDev& in = P.inst[P.grain[P.node_grain[d]].inst];
+    float rf[D];
+    ldf<D>(P.curf, d, rf);
+    int32_t ci[3] = {0, 0, 0};
+    for (int c = 0; c < D; ++c) ci[c] = cell_coord(rf[c], in.inv_cell_f, in.dims[c]);
+    const uint32_t key = in.table_off + ((uint32_t)ci[2] * in.dims[1] + (uint32_t)ci[1]) * in.dims[0] + (uint32_t)ci[0];
+    P.cell_key[d] = key;
+    P.cell_rank[d] = atomicAdd(&P.cell_count[key], 1u);
+  }
+  if (!grid_barrier(P, &ok)) return;
+  // 2. tile sums of the counts
+  const uint32_t ntiles = cdiv_dev(P.table_total, SCAN_TILE);
+  for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const uint32_t base = tile * SCAN_TILE + threadIdx.x * SCAN_PER;
+    uint32_t sum = 0;
+    for (int k = 0; k < SCAN_PER; ++k) {
+      const uint32_t i = base + k;
+      if (i < P.table_total) sum += P.cell_count[i];
+    }
+    uint32_t tot;
+    block_excl_scan(sum, ws, &tot);
+    if (threadIdx.x == 0) P.scan_tile_sum[tile] = tot;
+    __syncthreads();
+  }
+  if (!grid_barrier(P, &ok)) return;
+  // 3. exclusive scan of the tile sums (block 0)
+  if (blockIdx.x == 0) {
+    uint32_t carry = 0;
+    for (uint32_t b0 = 0; b0 < ntiles; b0 += SCAN_THREADS) {
+      const uint32_t i = b0 + threadIdx.x;
+      const uint32_t v = i < ntiles ? ((volatile uint32_t*)P.scan_tile_sum)[i] : 0;
+      uint32_t t2;
+      const uint32_t ex = block_excl_scan(v, ws, &t2);
+      __syncthreads();
+      if (i < ntiles) P.scan_tile_sum[i] = carry + ex;
+      carry += t2;
+      __syncthreads();
+    }
+  }
+  (void)last;
+  if (!grid_barrier(P, &ok)) return;
+  // 4. cell starts, counts cleared for the next build
+  for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const uint32_t base = tile * SCAN_TILE + threadIdx.x * SCAN_PER;
+    uint32_t v[SCAN_PER], sum = 0;
+    for (int k = 0; k < SCAN_PER; ++k) {
+      const uint32_t i = base + k;
+      v[k] = i < P.table_total ? P.cell_count[i] : 0;
+      sum += v[k];
+    }
+    uint32_t ex = block_excl_scan(sum, ws, nullptr) + ((volatile uint32_t*)P.scan_tile_sum)[tile];
+    for (int k = 0; k < SCAN_PER; ++k) {
+      const uint32_t i = base + k;
+      if (i < P.table_total) {
+        P.cell_start[i] = ex;
+        P.cell_count[i] = 0;
+      }
+      ex += v[k];
+    }
+    __syncthreads();
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) P.cell_start[P.table_total] = P.N;
+  if (!grid_barrier(P, &ok)) return;
+  // 5. scatter
+  for (uint32_t d = blockIdx.x * blockDim.x + threadIdx.x; d < P.N; d += nthr)
+    P.sorted[P.cell_start[P.cell_key[d]] + P.cell_rank[d]] = d;
+}
+
 // Grid build shared by both precisions: exclusive scan of the bucket counts, then scatter; with
 // candidate lists also the grid keys (before) and the list rebuild (after), all of them returning
 // at once on steps that need no rebuild.
 template <int D>
 inline void launch_grid_build(const Dev& P, cudaStream_t s, uint64_t* launches, bool pdl = false) {
   const uint32_t ntiles = cdiv(P.table_total, SCAN_TILE);
+  if (P.cand_q && P.coop_blocks) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(P.coop_blocks);
+    cfg.blockDim = dim3(SCAN_THREADS);
+    cfg.stream = s;
+    cudaLaunchAttribute at[2];
+    at[0].id = cudaLaunchAttributeCooperative;
+    at[0].val.cooperative = 1;
+    at[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[1].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = pdl ? 2 : 1;
+    cudaLaunchKernelEx(&cfg, k_grid_coop<D>, P);
+    launch_k(k_cand_build<D>, cdiv(P.N, 128), 128, 0, s, pdl, P);
+    *launches += 2;
+    return;
+  }
   if (P.cand_q) {
     launch_k(k_keys<D>, cdiv(P.N, 256), 256, 0, s, pdl, P);
     *launches += 1;

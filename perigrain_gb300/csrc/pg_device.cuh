@@ -149,6 +149,8 @@ struct Dev {
   uint32_t *cell_key, *cell_rank, *cell_count, *cell_start, *sorted;
   uint32_t *scan_tile_sum;
   uint32_t *scan_done;
+  uint32_t* gbar;      // [2] grid barrier of the cooperative grid build: arrivals, generation
+  uint32_t coop_blocks;  // blocks of that launch (all resident), 0 = separate grid kernels
   // bonds (SELL-32)
   uint32_t *chunk_slot, *chunk_deg, *chunk_word, *node_deg;
   uint32_t* bcol;

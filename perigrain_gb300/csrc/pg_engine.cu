@@ -770,6 +770,9 @@ static int create_impl(const pg_setup_desc* s, const pg_config* cfg_in, pg_handl
     CU(h->dalloc(&P.cand_n, N));
     CU(h->dalloc(&P.disp_b, (size_t)N * SF));
     CU(h->dalloc(&P.rebuild, 1));
+    CU(h->dalloc(&P.gbar, 2));
+    CU(cudaMemset(P.gbar, 0, 8));
+    P.coop_blocks = grid_coop_blocks(P, h->device);
     CU(cudaMemset(P.cand_n, 0, N));
     CU(cudaMemset(P.disp_b, 0, (size_t)N * SF * 4));
     const uint32_t one = 1;

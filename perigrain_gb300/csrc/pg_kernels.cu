@@ -15,6 +15,7 @@
 // reference performs, in the reference's order, so the non-wall path is bit-exact.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 
 #include "pg_common.cuh"
@@ -587,6 +588,18 @@ void launch_step_timed(const Dev& P, const LaunchCfg& L, cudaStream_t s, uint64_
   } else {
     launch_step_t<3>(P, L, s, launches, e0, e1);
   }
+}
+
+uint32_t grid_coop_blocks(const Dev& P, int device) {
+  int per_sm = 0, sms = 0, coop = 0;
+  const void* k = P.dim == 2 ? (const void*)k_grid_coop<2> : (const void*)k_grid_coop<3>;
+  if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device) != cudaSuccess || !coop) return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, SCAN_THREADS, 0) != cudaSuccess || per_sm < 1) return 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || sms < 1) return 0;
+  const uint32_t want = std::max(cdiv(P.N, SCAN_THREADS), cdiv(P.table_total, SCAN_TILE));
+  // two blocks per SM: enough threads for the light phases, few blocks to schedule on the (common)
+  // steps without a rebuild
+  return std::max(1u, std::min((uint32_t)(std::min(per_sm, 2) * sms), want));
 }
 
 const void* force_kernel_ptr(uint32_t dim) {

@@ -42,5 +42,8 @@ void launch_step(const Dev& P, const LaunchCfg& L, cudaStream_t s, uint64_t* lau
 void launch_step_timed(const Dev& P, const LaunchCfg& L, cudaStream_t s, uint64_t* launches,
                        cudaEvent_t e0, cudaEvent_t e1);
 const void* force_kernel_ptr(uint32_t dim);
+// Blocks of the cooperative grid build (k_grid_coop): every block resident at once (occupancy x
+// SMs), no more than the work needs; 0 when the device has no cooperative launch.
+uint32_t grid_coop_blocks(const Dev& P, int device);
 
 }  // namespace pg
