@@ -345,6 +345,73 @@ def postprocess_bench(sim, setup, repeats=20):
                                        % cpu_s}}
 
 
+class _QuietStdout:
+    """Sends file descriptor 1 to /dev/null (the drop-in driver prints its progress table there)."""
+
+    def __enter__(self):
+        sys.stdout.flush()
+        self.fd = os.dup(1)
+        self.nul = os.open(os.devnull, os.O_WRONLY)
+        os.dup2(self.nul, 1)
+
+    def __exit__(self, *exc):
+        import ctypes
+        ctypes.CDLL(None).fflush(None)
+        os.dup2(self.fd, 1)
+        os.close(self.fd)
+        os.close(self.nul)
+
+
+def dropin_bench(steps=2000, modulo=100):
+    """The drop-in process contract (pg_run_simulation: config/main.conf and data/hdf5/all.h5 in,
+    output/hdf5/ out, as bin/simulate2d runs it) in-process on the 2D settling workload, mixed
+    precision: node-steps/s with output off (save_file = 0) and with tc_/wall_ files every `modulo`
+    steps. The fixed cost of a run (reading all.h5, creating the engine, plotinfo.h5, run_time.h5)
+    is timed by 0-step runs and taken out."""
+    import shutil
+    import tempfile
+
+    from perigrain_gb300 import run_simulation, setups
+
+    spec = setups.WORKLOADS[1]
+    s = spec["build"]()
+    d = tempfile.mkdtemp(prefix="pg_dropin_")
+    try:
+        for sub in ("config", os.path.join("data", "hdf5"), os.path.join("output", "hdf5")):
+            os.makedirs(os.path.join(d, sub), exist_ok=True)
+        s.save_h5(os.path.join(d, "data", "hdf5", "all.h5"))
+
+        def run(T, save):
+            conf = {"timesteps": T, "modulo": modulo, "dt": spec["dt"], "save_file": save, "enable_fracture": 1,
+                    "allow_damping": 1, "allow_friction": 1, "self_contact": 1, "is_parallel": 1}
+            with open(os.path.join(d, "config", "main.conf"), "w") as f:
+                for k, v in conf.items():
+                    f.write("%s = %r\n" % (k, v))
+            t0 = time.perf_counter()
+            with _QuietStdout():
+                run_simulation(d, 2, "mixed")
+            return time.perf_counter() - t0
+
+        run(0, 0)
+        fixed = min(run(0, 0) for _ in range(2))
+        off = run(steps, 0)
+        on = run(steps, 1)
+        out = os.path.join(d, "output", "hdf5")
+        tc_bytes = os.path.getsize(os.path.join(out, "tc_00001.h5")) + os.path.getsize(os.path.join(out, "wall_00001.h5"))
+        n_out = steps // modulo
+        return {"workload": "%s: %d grains, %d nodes, %d bonds, through all.h5 and config/main.conf"
+                            % (spec["name"], s.n_grains, s.n_nodes, s.n_bonds),
+                "precision": "mixed", "steps": steps, "modulo": modulo, "fixed_ms": fixed * 1e3,
+                "no_output": {"value": s.n_nodes * steps / (off - fixed), "unit": METRIC, "ms": (off - fixed) * 1e3},
+                "with_output": {"value": s.n_nodes * steps / (on - fixed), "unit": METRIC, "ms": (on - fixed) * 1e3,
+                                "outputs": n_out, "bytes_per_output": tc_bytes},
+                "note": "files of one output are written while the GPU runs the next segment (pg_snapshot)"}
+    except Exception as e:  # reported in the line, the headline stands
+        return {"error": "%s: %s" % (type(e).__name__, e)}
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+
+
 def packing_bench(nx=800, ny=500, repeats=3):
     """Incircle packing (pg_pack_incenters) of a jittered 800 x 500-cell triangulated rectangle with
     the reference's default options (maximin nodal circles, boundary nodes included): circles per
@@ -561,22 +628,33 @@ def main():
     t0 = time.perf_counter()
     e2e_sim = Simulation(setup, **kw)
     t_created = time.perf_counter()
+    # a tc_ snapshot (CurrPos, vel, acc, force) every 100 steps, as the drop-in writes them: each is
+    # gathered on the device behind its steps and copied to page-locked host buffers while the next
+    # 100 steps run (pg_snapshot / pg_wait)
+    snap_items = ("CurrPos", "vel", "acc", "force")
+    bufs = e2e_sim.snapshot_buffers(snap_items)
     snaps = 0
     done = 0
     d2h = 0
-    t_dl = 0.0
+    t_wait = 0.0
+    pending = None
     while done < e2e_steps:
         n = min(100, e2e_steps - done)
         e2e_sim.step(n)
         done += n
-        td = time.perf_counter()
-        for f in ("CurrPos", "vel", "acc", "force"):
-            d2h += e2e_sim.field(f).nbytes
-        t_dl += time.perf_counter() - td
+        if pending is not None:
+            td = time.perf_counter()
+            got = pending.wait()
+            t_wait += time.perf_counter() - td
+            d2h += sum(got[f].nbytes for f in snap_items)
+        pending = e2e_sim.snapshot(snap_items, out=bufs)
         snaps += 1
+    td = time.perf_counter()
+    got = pending.wait()
+    t_wait += time.perf_counter() - td
+    d2h += sum(got[f].nbytes for f in snap_items)
     e2e_s = time.perf_counter() - t0
-    e2e_parts = {"create_ms": (t_created - t0) * 1e3, "download_ms": t_dl * 1e3,
-                 "steps_ms": (e2e_s - (t_created - t0) - t_dl) * 1e3}
+    e2e_parts = {"create_ms": (t_created - t0) * 1e3, "host_wait_ms": t_wait * 1e3}
     e2e_sim.close()
     h2d = sum(getattr(setup, f).nbytes for f in ("pos", "vol", "disp", "vel", "acc", "extforce", "bond_offset",
                                                    "bond_local"))
@@ -594,6 +672,7 @@ def main():
     adjoint = None if a.no_adjoint else adjoint_bench()
     packing_line = None if a.no_packing else packing_bench()
     bonds_line = None if a.no_packing else bonds_bench()
+    dropin_line = None if a.no_packing else dropin_bench()
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": ms_max / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -615,7 +694,8 @@ def main():
                                                cpu_info["nodes"], cpu_info["seconds"])},
         "e2e": {"value": setup.n_nodes * e2e_steps / e2e_s, "unit": METRIC, "steps": e2e_steps,
                 "h2d_bytes_per_step": h2d / e2e_steps, "d2h_bytes_per_step": d2h / e2e_steps,
-                "note": "pg_create from host arrays + %d steps + %d tc_ snapshot downloads (one every 100 steps)"
+                "note": "pg_create from host arrays + %d steps + %d tc_ snapshots (one every 100 steps, copied to "
+                        "page-locked host buffers while the next steps run)"
                         % (e2e_steps, snaps),
                 **e2e_parts},
         "gpu_launches": launches,
@@ -628,6 +708,7 @@ def main():
         "packing": packing_line,
         "bond_builder": bonds_line,
         "postprocess": post_line,
+        "dropin": dropin_line,
     }
     print(json.dumps(line), flush=True)
     if dist:

@@ -181,6 +181,35 @@ int pg_set_wall(pg_handle* h, const double* geom);
 /* Grain flags (set_movable_index / set_stoppable_index hooks, timeloop.h:612-627). */
 int pg_set_grain_flags(pg_handle* h, uint32_t grain, int32_t movable, int32_t stoppable);
 
+/* ---- asynchronous snapshots (the output step of run_timeloop, timeloop.h:881-1006) --------- */
+/* pg_snapshot enqueues, on the handle's stream behind the steps already issued, a copy of the
+ * state the tc_/wall_ files hold into device staging, and the copies from there into the
+ * caller's buffers on a second stream, so they overlap the steps issued after it. It does not
+ * block. pg_wait blocks until those copies are done, fills the items below and returns the
+ * device status word read at the snapshot, as pg_synchronize does. One snapshot is in flight
+ * per handle: pg_snapshot first completes one that has not been waited for. A null pointer
+ * skips its item. Buffers stay owned by the caller and must stay valid until pg_wait returns;
+ * page-locked buffers (pg_host_alloc, cudaHostAlloc) receive the copies directly, other memory
+ * through a page-locked bounce buffer that pg_wait copies out. Each item equals what the
+ * synchronous getter returns after the same steps. */
+typedef struct pg_snapshot_desc {
+  double* currpos;            /* [n_nodes*dim], as pg_get_field(PG_FIELD_CURRPOS) */
+  double* vel;                /* [n_nodes*dim] */
+  double* acc;                /* [n_nodes*dim] */
+  double* force;              /* [n_nodes*dim], force density */
+  double* disp;               /* [n_nodes*dim] */
+  uint8_t* bond_alive;        /* [n_bonds], as pg_get_bond_alive */
+  double* wall;               /* [n_instances*2*dim], as pg_get_wall */
+  double* reaction;           /* [n_instances*2*dim*dim], as pg_get_reaction */
+  uint64_t* too_close_events; /* as pg_get_device_status */
+  uint64_t* last_step;        /* index of the last step taken before the snapshot */
+} pg_snapshot_desc;
+int pg_snapshot(pg_handle* h, const pg_snapshot_desc* d);
+int pg_wait(pg_handle* h);
+/* Page-locked host memory (for snapshot buffers); pg_host_free releases it. */
+int pg_host_alloc(size_t bytes, void** out);
+int pg_host_free(void* p);
+
 /* ---- diagnostics ---------------------------------------------------------------------------- */
 /* Per-step contact-pair log (needs cfg.record_pairs): for the last `n` steps ending at the
  * last completed step, count[k] = number of node pairs that passed the contact test

@@ -5,7 +5,7 @@ with bond breaking, node-node and analytic-wall contact with damping and frictio
 velocity-Verlet update, as hand-written CUDA kernels behind a C ABI (include/perigrain.h).
 """
 from . import _native
-from .engine import Simulation, device_count, run_simulation
+from .engine import Simulation, Snapshot, device_count, pinned_empty, run_simulation
 from . import setups
 
-__all__ = ["Simulation", "run_simulation", "device_count", "setups", "_native"]
+__all__ = ["Simulation", "Snapshot", "pinned_empty", "run_simulation", "device_count", "setups", "_native"]

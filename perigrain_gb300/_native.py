@@ -84,6 +84,12 @@ class Conf(C.Structure):
     _fields_ = CONF_FIELDS
 
 
+class SnapshotDesc(C.Structure):
+    _fields_ = [("currpos", C.c_void_p), ("vel", C.c_void_p), ("acc", C.c_void_p), ("force", C.c_void_p),
+                ("disp", C.c_void_p), ("bond_alive", C.c_void_p), ("wall", C.c_void_p), ("reaction", C.c_void_p),
+                ("too_close_events", C.c_void_p), ("last_step", C.c_void_p)]
+
+
 # (name, restype, argtypes) of every exported function; tests check that each is exported.
 PROTOTYPES = [
     ("pg_version", C.c_int, []),
@@ -107,6 +113,10 @@ PROTOTYPES = [
     ("pg_get_wall", C.c_int, [C.c_void_p, f64p]),
     ("pg_set_wall", C.c_int, [C.c_void_p, f64p]),
     ("pg_set_grain_flags", C.c_int, [C.c_void_p, C.c_uint32, C.c_int32, C.c_int32]),
+    ("pg_snapshot", C.c_int, [C.c_void_p, C.POINTER(SnapshotDesc)]),
+    ("pg_wait", C.c_int, [C.c_void_p]),
+    ("pg_host_alloc", C.c_int, [C.c_size_t, C.POINTER(C.c_void_p)]),
+    ("pg_host_free", C.c_int, [C.c_void_p]),
     ("pg_get_pair_log", C.c_int, [C.c_void_p, C.c_uint32, u64p, u64p]),
     ("pg_get_device_status", C.c_int, [C.c_void_p, i32p, u64p]),
     ("pg_get_launch_count", C.c_int, [C.c_void_p, u64p]),

@@ -796,17 +796,19 @@ int pg_destroy(pg_handle* h) {
 
 }  // extern "C"
 
+int device_status_fail(int32_t st) {
+  if (!st) return PG_OK;
+  std::string m = "device reported: ";
+  m += pg_status_string(st);
+  if (st == PG_ECAPACITY) m += " (contact candidates per node, or wall records per step)";
+  return fail(st, m);
+}
+
 int check_device_status(pg_handle* h) {
   int32_t st = 0;
   CU(cudaMemcpyAsync(&st, h->P.status, 4, cudaMemcpyDeviceToHost, h->stream));
   CU(cudaStreamSynchronize(h->stream));
-  if (st) {
-    std::string m = "device reported: ";
-    m += pg_status_string(st);
-    if (st == PG_ECAPACITY) m += " (contact candidates per node, or wall records per step)";
-    return fail(st, m);
-  }
-  return PG_OK;
+  return device_status_fail(st);
 }
 
 extern "C" {

@@ -112,6 +112,42 @@ struct GradState {
   }
 };
 
+// An asynchronous snapshot (pg_snapshot / pg_wait): device staging written on the handle's
+// stream, copied to the host on `copy`.
+struct SnapState {
+  cudaStream_t copy = nullptr;
+  cudaEvent_t staged = nullptr, copied = nullptr;
+  char* stage = nullptr;  // device: requested fields, then alive bytes
+  size_t stage_bytes = 0;
+  char* small_dev = nullptr;   // device: reaction, wall, status, too_close
+  char* small_host = nullptr;  // page-locked host copy of small_dev
+  size_t small_bytes = 0;
+  char* bounce = nullptr;  // page-locked host copy for caller buffers that are not page-locked
+  size_t bounce_bytes = 0;
+  uint64_t* bond_offset = nullptr;  // device copy of the CSR offsets (alive bytes in CSR order)
+  bool pending = false;
+  pg_snapshot_desc d{};
+  uint64_t last_step = 0;
+  struct CopyOut {
+    void* dst;
+    const char* src;
+    size_t bytes;
+  };
+  std::vector<CopyOut> out;  // bounce -> caller, done by pg_wait
+
+  ~SnapState() {
+    if (copy) cudaStreamSynchronize(copy);
+    if (staged) cudaEventDestroy(staged);
+    if (copied) cudaEventDestroy(copied);
+    if (copy) cudaStreamDestroy(copy);
+    cudaFree(stage);
+    cudaFree(small_dev);
+    cudaFree(bond_offset);
+    if (small_host) cudaFreeHost(small_host);
+    if (bounce) cudaFreeHost(bounce);
+  }
+};
+
 struct pg_handle {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -149,9 +185,11 @@ struct pg_handle {
   double* post_sum = nullptr;
   double* post_damage = nullptr;
   double* field_scratch = nullptr;  // [N][D] doubles: FP32 fields widened for pg_get_field
+  std::unique_ptr<SnapState> snap;
 
   ~pg_handle() {
     if (stream) cudaStreamSynchronize(stream);
+    snap.reset();
     grad.reset();
     for (int i = 0; i < 2; ++i)
       if (graph[i]) cudaGraphExecDestroy(graph[i]);
@@ -177,5 +215,7 @@ void set_vel(pg_handle* h, pg::Dev& P, int parity);
 void enqueue_step(pg_handle* h, int parity, uint64_t* launches);
 int build_graphs(pg_handle* h);
 int check_device_status(pg_handle* h);
+// PG_OK for st == 0, else records the device status message and returns st.
+int device_status_fail(int32_t st);
 // Force a rebuild of the contact candidate lists at the next step (no-op without lists).
 int request_list_rebuild(pg_handle* h);

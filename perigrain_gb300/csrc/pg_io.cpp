@@ -577,12 +577,9 @@ extern "C" int pg_setup_save(pg_setup* s, const char* path) {
 // =============================================================================================
 // output
 // =============================================================================================
-static int write_tc(pg_handle* h, pg_setup* s, const std::string& dir, uint32_t counter,
-                    const std::vector<double>& cur, const std::vector<double>& vel,
-                    const std::vector<double>& acc, const std::vector<double>& force,
-                    const std::vector<uint8_t>& alive, const std::vector<double>& wall,
-                    const std::vector<double>& reaction, bool connectivity = true) {
-  (void)h;
+static int write_tc(pg_setup* s, const std::string& dir, uint32_t counter, const double* cur, const double* vel,
+                    const double* acc, const double* force, const uint8_t* alive, const double* wall,
+                    const double* reaction, bool connectivity = true) {
   const uint32_t D = s->dim;
   char buf[64];
   std::snprintf(buf, sizeof buf, "%05u", counter);
@@ -593,20 +590,20 @@ static int write_tc(pg_handle* h, pg_setup* s, const std::string& dir, uint32_t 
     std::string pre(gb);
     const uint32_t n0 = s->node_off[g], n = s->node_off[g + 1] - n0;
     w.create_group(pre);
-    w.add_dataset(pre + "CurrPos", h5l::DType::F64, {n, D}, cur.data() + (size_t)n0 * D);
-    w.add_dataset(pre + "vel", h5l::DType::F64, {n, D}, vel.data() + (size_t)n0 * D);
-    w.add_dataset(pre + "acc", h5l::DType::F64, {n, D}, acc.data() + (size_t)n0 * D);
-    w.add_dataset(pre + "force", h5l::DType::F64, {n, D}, force.data() + (size_t)n0 * D);
+    w.add_dataset(pre + "CurrPos", h5l::DType::F64, {n, D}, cur + (size_t)n0 * D);
+    w.add_dataset(pre + "vel", h5l::DType::F64, {n, D}, vel + (size_t)n0 * D);
+    w.add_dataset(pre + "acc", h5l::DType::F64, {n, D}, acc + (size_t)n0 * D);
+    w.add_dataset(pre + "force", h5l::DType::F64, {n, D}, force + (size_t)n0 * D);
     if (connectivity) {  // run_timeloop_worm writes none (timeloop.h:1283-1292)
       std::vector<uint32_t> conn;
-      rows_to_conn(s, g, alive.data(), &conn);
+      rows_to_conn(s, g, alive, &conn);
       w.add_dataset(pre + "Connectivity", h5l::DType::U32, {conn.size() / 2, 2}, conn.data());
     }
   }
   if (!w.write(dir + "/tc_" + buf + ".h5")) return iofail(PG_EIO, "cannot write " + dir + "/tc_" + buf + ".h5");
   h5l::Writer ww;
-  ww.add_dataset("wall_info", h5l::DType::F64, {2ull * D, 1}, wall.data());
-  ww.add_dataset("reaction", h5l::DType::F64, {2ull * D, D}, reaction.data());
+  ww.add_dataset("wall_info", h5l::DType::F64, {2ull * D, 1}, wall);
+  ww.add_dataset("reaction", h5l::DType::F64, {2ull * D, D}, reaction);
   if (!ww.write(dir + "/wall_" + buf + ".h5")) return iofail(PG_EIO, "cannot write wall file");
   return PG_OK;
 }
@@ -622,7 +619,8 @@ static int snapshot(pg_handle* h, pg_setup* s, const char* out_dir, uint32_t cou
       (rc = pg_get_bond_alive(h, alive.data())) || (rc = pg_get_wall(h, wall.data())) ||
       (rc = pg_get_reaction(h, reaction.data())))
     return iofail(rc, pg_last_error());
-  return write_tc(h, s, out_dir, counter, cur, vel, acc, force, alive, wall, reaction, connectivity);
+  return write_tc(s, out_dir, counter, cur.data(), vel.data(), acc.data(), force.data(), alive.data(), wall.data(),
+                  reaction.data(), connectivity);
 }
 
 extern "C" int pg_write_snapshot(pg_handle* h, pg_setup* s, const char* out_dir, uint32_t counter) {
@@ -775,18 +773,107 @@ extern "C" int pg_run_simulation(const char* root_c, uint32_t dim, int32_t preci
   std::vector<double> ts_time, ts_wall, ts_react, ts_phi, ts_dmg, ts_force, ts_vel, ts_acc, ts_pos, ts_fsum;
   const uint32_t T = C.timesteps;
   uint64_t too_close_seen = 0;
+
+  // Output is pipelined: the snapshot of output step e is taken on the device (pg_snapshot) and its
+  // files are written while the GPU computes the next segment; stdout keeps the reference's order
+  // (a hook's message after the output line of the steps before it).
+  struct HostBuf {
+    void* p = nullptr;
+    ~HostBuf() { pg_host_free(p); }
+  };
+  const size_t nd = (size_t)S->N * dim;
+  HostBuf hb_fields, hb_alive;
+  double *o_cur = nullptr, *o_vel = nullptr, *o_acc = nullptr, *o_force = nullptr;
+  uint8_t* o_alive = nullptr;
+  std::vector<double> o_wall(2 * dim), o_react((size_t)2 * dim * dim);
+  uint64_t o_too_close = 0;
+  if (C.save_file && C.modulo) {
+    if ((rc = pg_host_alloc(4 * nd * sizeof(double), &hb_fields.p))) return iofail(rc, pg_last_error());
+    if ((rc = pg_host_alloc(S->bond_local.size() + 1, &hb_alive.p))) return iofail(rc, pg_last_error());
+    o_cur = static_cast<double*>(hb_fields.p);
+    o_vel = o_cur + nd;
+    o_acc = o_vel + nd;
+    o_force = o_acc + nd;
+    o_alive = static_cast<uint8_t*>(hb_alive.p);
+  }
+  struct Pending {
+    bool on = false;
+    uint32_t counter = 0, e = 0;
+    std::vector<double> v, a, x, f, dmg, fs, phi;  // post-processing at the output step
+  } pend;
+  auto finish_output = [&]() -> int {
+    if (!pend.on) return PG_OK;
+    pend.on = false;
+    int r = pg_wait(H);
+    if (r) return iofail(r, pg_last_error());
+    for (; too_close_seen < o_too_close; ++too_close_seen) std::cout << "Error: nodes too close" << std::endl;
+    r = write_tc(S, out, pend.counter, o_cur, o_vel, o_acc, o_force, o_alive, o_wall.data(), o_react.data(), !worm);
+    if (r) return r;
+    if (tsd) {
+      ts_time.push_back((double)pend.counter * C.dt * (double)C.modulo);  // extract_bulk: t * dt * modulo
+      ts_wall.insert(ts_wall.end(), o_wall.begin(), o_wall.end());
+      ts_react.insert(ts_react.end(), o_react.begin(), o_react.end());
+      ts_phi.push_back(pend.phi[0]);
+      ts_dmg.insert(ts_dmg.end(), pend.dmg.begin(), pend.dmg.end());
+      ts_force.insert(ts_force.end(), pend.f.begin(), pend.f.end());
+      ts_vel.insert(ts_vel.end(), pend.v.begin(), pend.v.end());
+      ts_acc.insert(ts_acc.end(), pend.a.begin(), pend.a.end());
+      ts_pos.insert(ts_pos.end(), pend.x.begin(), pend.x.end());
+      ts_fsum.insert(ts_fsum.end(), pend.fs.begin(), pend.fs.end());
+    }
+    auto stop_time = std::chrono::system_clock::now();
+    auto duration = std::chrono::duration_cast<std::chrono::milliseconds>(stop_time - start_time);
+    start_time = stop_time;
+    int avgsteps = 10;
+    double avg_duration = 0;
+    if (run_time.size() >= 10) {
+      for (size_t cc = run_time.size() - avgsteps; cc < run_time.size(); ++cc) avg_duration += run_time[cc];
+      avg_duration /= avgsteps;
+    }
+    int rem_counts = (int)last_counter - (int)pend.counter;
+    if (worm) {
+      // the worm loop's line (timeloop.h:1331-1350): t, counter, duration/100, remaining m s, ctime
+      avg_duration = 0;
+      if (run_time.size() >= 10)
+        for (size_t cc = run_time.size() - avgsteps; cc < run_time.size(); ++cc) avg_duration += run_time[cc];
+      avg_duration /= avgsteps;
+      const double rem_min = (rem_counts * avg_duration) / 1e3 / 60;
+      time_t now = time(NULL);
+      std::cout << pend.e << "\t" << pend.counter << "\t" << duration.count() / 100 << "\t" << (int)rem_min << "m"
+                << (rem_min - (int)rem_min) * 60 << "s" << "\t" << ctime(&now);
+    } else {
+      int rem_s = (int)((rem_counts * avg_duration) / 1e3);
+      char rem[32];
+      std::snprintf(rem, sizeof rem, "%02d:%02d:%02d", (rem_s / 60) / 60, (rem_s / 60) % 60, rem_s % 60);
+      time_t now = time(NULL);
+      char ts[80];
+      strftime(ts, sizeof ts, "%F-%T", localtime(&now));
+      std::cout << std::left << std::setw(column_w) << pend.e << std::left << std::setw(column_w) << pend.counter
+                << std::left << std::setw(column_w) << (double)duration.count() / 1000 << std::left
+                << std::setw(column_w + 5) << rem << std::left << std::setw(column_w + 10) << ts << std::endl;
+    }
+    run_time.push_back((double)duration.count());
+    t_ind.push_back(pend.e);
+    return PG_OK;
+  };
+
   uint32_t t = 1;
   while (t <= T) {
+    const bool hook_movable = !worm && C.set_movable_index != -1 && (uint32_t)C.set_movable_timestep == t;
+    const bool hook_stoppable = !worm && C.set_stoppable_index != -1 && (uint32_t)C.set_stoppable_timestep == t;
+    const bool hook_reset = !worm && C.reset_partzero_y && C.reset_partzero_y_timestep == t && S->G > 1;
+    if (hook_movable || hook_stoppable || hook_reset)
+      if ((rc = finish_output())) return rc;
     // hooks at the start of step t (timeloop.h:612-650); the worm loop has none
-    if (!worm && C.set_movable_index != -1 && (uint32_t)C.set_movable_timestep == t) {
+    if (hook_movable) {
       std::cout << "Setting particle " << C.set_movable_index << " to movable on timestep " << t << std::endl;
       if ((rc = pg_set_grain_flags(H, (uint32_t)C.set_movable_index, 1, -1))) return iofail(rc, pg_last_error());
     }
-    if (!worm && C.set_stoppable_index != -1 && (uint32_t)C.set_stoppable_timestep == t) {
+    if (hook_stoppable) {
       std::cout << "Setting particle " << C.set_stoppable_index << " to stoppable on timestep " << t << std::endl;
       if ((rc = pg_set_grain_flags(H, (uint32_t)C.set_stoppable_index, -1, 1))) return iofail(rc, pg_last_error());
     }
-    if (!worm && C.reset_partzero_y && C.reset_partzero_y_timestep == t && S->G > 1) {
+    if (hook_reset) {
       std::vector<double> pos((size_t)S->N * dim), disp(pos.size());
       if ((rc = pg_get_field(H, PG_FIELD_POS, pos.data())) || (rc = pg_get_field(H, PG_FIELD_DISP, disp.data())))
         return iofail(rc, pg_last_error());
@@ -817,74 +904,44 @@ extern "C" int pg_run_simulation(const char* root_c, uint32_t dim, int32_t preci
     if (!worm && C.reset_partzero_y) hook(C.reset_partzero_y_timestep);
     if (e < t) e = t;
     if ((rc = pg_step(H, e - t + 1))) return iofail(rc, pg_last_error());
+    // the previous output's files are written while these steps run
+    if ((rc = finish_output())) return rc;
     t = e + 1;
     if (C.save_file && C.modulo && (e % C.modulo) == 0) {
-      if ((rc = pg_synchronize(H))) return iofail(rc, pg_last_error());
-      uint64_t tc = 0;
-      pg_get_device_status(H, nullptr, &tc);
-      for (; too_close_seen < tc; ++too_close_seen) std::cout << "Error: nodes too close" << std::endl;
-      if ((rc = snapshot(H, S, out.c_str(), counter, !worm))) return rc;
+      pg_snapshot_desc sd{};
+      sd.currpos = o_cur;
+      sd.vel = o_vel;
+      sd.acc = o_acc;
+      sd.force = o_force;
+      sd.bond_alive = worm ? nullptr : o_alive;
+      sd.wall = o_wall.data();
+      sd.reaction = o_react.data();
+      sd.too_close_events = &o_too_close;
+      if ((rc = pg_snapshot(H, &sd))) return iofail(rc, pg_last_error());
+      pend.on = true;
+      pend.counter = counter;
+      pend.e = e;
       if (tsd) {
         const uint32_t G = S->G;
-        std::vector<double> v((size_t)G * dim), a(v.size()), x(v.size()), f(v.size()), dmg(G), fs(dim), phi(1),
-            wl(NSd), re((size_t)NSd * dim);
+        pend.v.assign((size_t)G * dim, 0.0);
+        pend.a = pend.x = pend.f = pend.v;
+        pend.dmg.assign(G, 0.0);
+        pend.fs.assign(dim, 0.0);
+        pend.phi.assign(1, 0.0);
         pg_post po{};
-        po.grain_mean_vel = v.data();
-        po.grain_mean_acc = a.data();
-        po.grain_mean_currpos = x.data();
-        po.grain_force = f.data();
-        po.grain_damage = dmg.data();
-        po.inertial_force = fs.data();
-        po.volume_fraction = phi.data();
-        if ((rc = pg_postprocess(H, &po)) || (rc = pg_get_wall(H, wl.data())) || (rc = pg_get_reaction(H, re.data())))
-          return iofail(rc, pg_last_error());
-        ts_time.push_back((double)counter * C.dt * (double)C.modulo);  // extract_bulk: t * dt * modulo
-        ts_wall.insert(ts_wall.end(), wl.begin(), wl.end());
-        ts_react.insert(ts_react.end(), re.begin(), re.end());
-        ts_phi.push_back(phi[0]);
-        ts_dmg.insert(ts_dmg.end(), dmg.begin(), dmg.end());
-        ts_force.insert(ts_force.end(), f.begin(), f.end());
-        ts_vel.insert(ts_vel.end(), v.begin(), v.end());
-        ts_acc.insert(ts_acc.end(), a.begin(), a.end());
-        ts_pos.insert(ts_pos.end(), x.begin(), x.end());
-        ts_fsum.insert(ts_fsum.end(), fs.begin(), fs.end());
+        po.grain_mean_vel = pend.v.data();
+        po.grain_mean_acc = pend.a.data();
+        po.grain_mean_currpos = pend.x.data();
+        po.grain_force = pend.f.data();
+        po.grain_damage = pend.dmg.data();
+        po.inertial_force = pend.fs.data();
+        po.volume_fraction = pend.phi.data();
+        if ((rc = pg_postprocess(H, &po))) return iofail(rc, pg_last_error());
       }
-      auto stop_time = std::chrono::system_clock::now();
-      auto duration = std::chrono::duration_cast<std::chrono::milliseconds>(stop_time - start_time);
-      start_time = stop_time;
-      int avgsteps = 10;
-      double avg_duration = 0;
-      if (run_time.size() >= 10) {
-        for (size_t cc = run_time.size() - avgsteps; cc < run_time.size(); ++cc) avg_duration += run_time[cc];
-        avg_duration /= avgsteps;
-      }
-      int rem_counts = (int)last_counter - (int)counter;
-      if (worm) {
-        // the worm loop's line (timeloop.h:1331-1350): t, counter, duration/100, remaining m s, ctime
-        avg_duration = 0;
-        if (run_time.size() >= 10)
-          for (size_t cc = run_time.size() - avgsteps; cc < run_time.size(); ++cc) avg_duration += run_time[cc];
-        avg_duration /= avgsteps;
-        const double rem_min = (rem_counts * avg_duration) / 1e3 / 60;
-        time_t now = time(NULL);
-        std::cout << e << "\t" << counter << "\t" << duration.count() / 100 << "\t" << (int)rem_min << "m"
-                  << (rem_min - (int)rem_min) * 60 << "s" << "\t" << ctime(&now);
-      } else {
-      int rem_s = (int)((rem_counts * avg_duration) / 1e3);
-      char rem[32];
-      std::snprintf(rem, sizeof rem, "%02d:%02d:%02d", (rem_s / 60) / 60, (rem_s / 60) % 60, rem_s % 60);
-      time_t now = time(NULL);
-      char ts[80];
-      strftime(ts, sizeof ts, "%F-%T", localtime(&now));
-      std::cout << std::left << std::setw(column_w) << e << std::left << std::setw(column_w) << counter
-                << std::left << std::setw(column_w) << (double)duration.count() / 1000 << std::left
-                << std::setw(column_w + 5) << rem << std::left << std::setw(column_w + 10) << ts << std::endl;
-      }
-      run_time.push_back((double)duration.count());
-      t_ind.push_back(e);
       ++counter;
     }
   }
+  if ((rc = finish_output())) return rc;
   if ((rc = pg_synchronize(H))) return iofail(rc, pg_last_error());
   {
     h5l::Writer w;

@@ -8,6 +8,7 @@ time steps; fields come back in the reference's node order. :func:`run_simulatio
 output/hdf5/*.h5 out).
 """
 import ctypes as C
+import weakref
 
 import numpy as np
 
@@ -53,6 +54,7 @@ class Simulation:
         if getattr(self, "h", None):
             N.lib().pg_destroy(self.h)
             self.h = None
+            self._pending = None
 
     def __del__(self):
         try:
@@ -116,6 +118,62 @@ class Simulation:
         out = np.empty((self.setup.n_instances, 2 * self.dim), np.float64)
         N.check(N.lib().pg_get_wall(self.h, N.ptr(out, C.c_double)))
         return out
+
+    SNAPSHOT_ITEMS = ("CurrPos", "vel", "acc", "force", "disp", "bond_alive", "wall", "reaction")
+
+    def snapshot_buffers(self, items=("CurrPos", "vel", "acc", "force")):
+        """Page-locked host arrays for :meth:`snapshot` (the copies then go straight into them)."""
+        n, d = self.setup.n_nodes, self.dim
+        shapes = {"bond_alive": ((max(1, self.setup.n_bonds),), np.uint8),
+                  "wall": ((self.setup.n_instances, 2 * d), np.float64),
+                  "reaction": ((self.setup.n_instances, 2 * d, d), np.float64)}
+        out = {}
+        for k in items:
+            shape, dt = shapes.get(k, ((n, d), np.float64))
+            out[k] = pinned_empty(shape, dt)
+        return out
+
+    def snapshot(self, items=("CurrPos", "vel", "acc", "force"), out=None):
+        """Enqueue an asynchronous snapshot (pg_snapshot) of the state after the steps issued so far
+        and return a :class:`Snapshot`; its ``wait()`` returns the arrays. The copies overlap steps
+        issued before ``wait()``. ``out`` (e.g. from :meth:`snapshot_buffers`) receives the copies;
+        by default new arrays are made."""
+        bad = [k for k in items if k not in self.SNAPSHOT_ITEMS]
+        if bad:
+            raise ValueError("unknown snapshot item(s): %s" % bad)
+        n, d = self.setup.n_nodes, self.dim
+        arrs = {}
+        for k in items:
+            if out is not None and k in out:
+                arrs[k] = out[k]
+            elif k == "bond_alive":
+                arrs[k] = np.empty(max(1, self.setup.n_bonds), np.uint8)
+            elif k == "wall":
+                arrs[k] = np.empty((self.setup.n_instances, 2 * d), np.float64)
+            elif k == "reaction":
+                arrs[k] = np.empty((self.setup.n_instances, 2 * d, d), np.float64)
+            else:
+                arrs[k] = np.empty((n, d), np.float64)
+        for k, a in arrs.items():
+            want = np.uint8 if k == "bond_alive" else np.float64
+            if a.dtype != want or not a.flags.c_contiguous:
+                raise ValueError("snapshot buffer %s: C-contiguous %s expected" % (k, np.dtype(want).name))
+        snap = Snapshot(self, arrs)
+        desc = N.SnapshotDesc()
+        names = {"CurrPos": "currpos", "vel": "vel", "acc": "acc", "force": "force", "disp": "disp",
+                 "bond_alive": "bond_alive", "wall": "wall", "reaction": "reaction"}
+        for k, a in arrs.items():
+            setattr(desc, names[k], a.ctypes.data)
+        desc.too_close_events = C.addressof(snap._too_close)
+        desc.last_step = C.addressof(snap._last_step)
+        # the engine writes into the buffers of a snapshot in flight until it is waited for (or the
+        # next snapshot completes it): keep them alive until then
+        prev = getattr(self, "_pending", None)
+        N.check(N.lib().pg_snapshot(self.h, C.byref(desc)))
+        if prev is not None:
+            prev._done = True
+        self._pending = snap
+        return snap
 
     def set_grain_flags(self, grain, movable=-1, stoppable=-1):
         N.check(N.lib().pg_set_grain_flags(self.h, int(grain), int(movable), int(stoppable)))
@@ -188,3 +246,41 @@ def device_count():
     n = C.c_int32()
     rc = N.lib().pg_device_count(C.byref(n))
     return n.value if rc == N.PG_OK else 0
+
+
+class Snapshot:
+    """An asynchronous snapshot in flight (pg_snapshot); ``wait()`` (pg_wait) returns a dict of the
+    requested arrays plus ``too_close_events`` and ``last_step``. The arrays hold the state after
+    the steps issued before the snapshot, whatever was issued after it."""
+
+    def __init__(self, sim, arrays):
+        self._sim = sim
+        self.arrays = arrays
+        self._too_close = C.c_uint64()
+        self._last_step = C.c_uint64()
+        self._done = False
+
+    def wait(self):
+        if not self._done:
+            self._done = True
+            if getattr(self._sim, "_pending", None) is self:
+                self._sim._pending = None
+            N.check(N.lib().pg_wait(self._sim.h))
+        out = dict(self.arrays)
+        if "bond_alive" in out:
+            out["bond_alive"] = out["bond_alive"][: self._sim.setup.n_bonds]
+        out["too_close_events"] = self._too_close.value
+        out["last_step"] = self._last_step.value
+        return out
+
+
+def pinned_empty(shape, dtype=np.float64):
+    """A numpy array in page-locked host memory (pg_host_alloc), freed with the array."""
+    dtype = np.dtype(dtype)
+    nbytes = max(1, int(np.prod(shape)) * dtype.itemsize)
+    L = N.lib()
+    p = C.c_void_p()
+    N.check(L.pg_host_alloc(nbytes, C.byref(p)))
+    buf = (C.c_uint8 * nbytes).from_address(p.value)
+    weakref.finalize(buf, L.pg_host_free, C.c_void_p(p.value))
+    return np.frombuffer(buf, dtype, count=int(np.prod(shape))).reshape(shape)
