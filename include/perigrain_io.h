@@ -3,7 +3,7 @@
  *
  *   config/main.conf   key = value parser          (reference src/read/read_config.h:14-297)
  *   data/hdf5/all.h5   setup loader                (src/read/load_hdf5.h:28-201)
- *   output/hdf5/*.h5   plotinfo / tc_ / wall_ / run_time writers (src/particle/timeloop.h:560-582,
+ *   output/hdf5/       plotinfo / tc_ / wall_ / run_time writers (src/particle/timeloop.h:560-582,
  *                      :881-1014)
  *   run_timeloop       the whole driver on top of perigrain.h (src/particle/timeloop.h:501-1015,
  *                      run/simulate2d.cpp:31-94)
@@ -78,6 +78,12 @@ int pg_setup_set_connectivity(pg_setup* s, uint32_t grain, const uint32_t* conn,
 /* ---- output ------------------------------------------------------------------------------ */
 /* Write tc_%05u.h5 + wall_%05u.h5 for `counter` into out_dir from a live handle. */
 int pg_write_snapshot(pg_handle* h, pg_setup* s, const char* out_dir, uint32_t counter);
+/* The same files from host arrays laid out as pg_snapshot_desc fills them: n_nodes*dim fields,
+ * bond_alive in CSR order (null: every bond of the setup is intact), wall [2*dim], reaction
+ * [2*dim*dim]. connectivity = 0 leaves Connectivity out, as run_timeloop_worm does. */
+int pg_write_tc(pg_setup* s, const char* out_dir, uint32_t counter, const double* currpos, const double* vel,
+                const double* acc, const double* force, const uint8_t* bond_alive, const double* wall,
+                const double* reaction, int32_t connectivity);
 
 /* ---- the driver -------------------------------------------------------------------------- */
 /* run/simulate{2,3}d: read <root>/config/main.conf and <root>/data/hdf5/all.h5, run the time

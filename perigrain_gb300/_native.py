@@ -156,6 +156,8 @@ PROTOTYPES = [
     ("pg_setup_save", C.c_int, [C.c_void_p, C.c_char_p]),
     ("pg_setup_set_connectivity", C.c_int, [C.c_void_p, C.c_uint32, u32p, C.c_uint64]),
     ("pg_write_snapshot", C.c_int, [C.c_void_p, C.c_void_p, C.c_char_p, C.c_uint32]),
+    ("pg_write_tc", C.c_int, [C.c_void_p, C.c_char_p, C.c_uint32, f64p, f64p, f64p, f64p, u8p, f64p, f64p,
+                              C.c_int32]),
     ("pg_run_simulation", C.c_int, [C.c_char_p, C.c_uint32, C.c_int32]),
     ("pg_h5w_new", C.c_void_p, []),
     ("pg_h5w_add", C.c_int, [C.c_void_p, C.c_char_p, C.c_int32, C.c_uint32, u64p, C.c_void_p]),

@@ -73,14 +73,14 @@ def build(verbose=False, force=False):
         o = os.path.join(BUILD, src + ".o")
         objs.append(o)
         if force or _stale(o, [s] + headers):
-            jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall",
+            jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-pthread", "-ffp-contract=off", "-Wall",
                          "-c", s, "-o", o])
     logs = []
     with ThreadPoolExecutor(max_workers=max(2, os.cpu_count() or 2)) as ex:
         for out in ex.map(_run, jobs):
             logs.append(out)
     if force or _stale(LIB, objs):
-        logs.append(_run([nvcc] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"]))
+        logs.append(_run([nvcc] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart", "-lpthread"]))
     for dim in (2, 3):
         exe = os.path.join(BIN, "simulate%dd" % dim)
         src = os.path.join(CSRC, "simulate.cpp")

@@ -49,6 +49,10 @@ struct Writer::Node {
   DType t = DType::F64;
   std::vector<uint64_t> dims;
   std::vector<uint8_t> data;
+  const uint8_t* ext = nullptr;  // borrowed data (add_dataset_ref), ext_bytes long
+  size_t ext_bytes = 0;
+  size_t nbytes() const { return ext ? ext_bytes : data.size(); }
+  const uint8_t* bytes() const { return ext ? ext : data.data(); }
 };
 
 Writer::Writer() : root_(new Node) {}
@@ -86,6 +90,16 @@ void Writer::create_group(const std::string& path) { make_group(path); }
 
 bool Writer::add_dataset(const std::string& path, DType t, const std::vector<uint64_t>& dims,
                          const void* data) {
+  return add(path, t, dims, data, true);
+}
+
+bool Writer::add_dataset_ref(const std::string& path, DType t, const std::vector<uint64_t>& dims,
+                             const void* data) {
+  return add(path, t, dims, data, false);
+}
+
+bool Writer::add(const std::string& path, DType t, const std::vector<uint64_t>& dims, const void* data,
+                 bool copy) {
   auto parts = split_path(path);
   if (parts.empty()) return false;
   std::string leaf = parts.back();
@@ -100,16 +114,35 @@ bool Writer::add_dataset(const std::string& path, DType t, const std::vector<uin
   uint64_t n = 1;
   for (auto x : dims) n *= x;
   size_t bytes = (size_t)n * dtype_size(t);
-  d->data.resize(bytes);
-  if (bytes) std::memcpy(d->data.data(), data, bytes);
+  if (copy || !bytes) {
+    d->data.resize(bytes);
+    if (bytes) std::memcpy(d->data.data(), data, bytes);
+  } else {
+    d->ext = static_cast<const uint8_t*>(data);
+    d->ext_bytes = bytes;
+  }
   g->children.emplace(leaf, std::move(d));
   return true;
 }
 
 namespace {
+// The file image: metadata bytes in `b`, with the borrowed dataset bytes as holes that are only
+// read when the file is written. pos() is the file offset; put64 patches the superblock, which
+// precedes every hole.
 struct Buf {
+  struct Hole {
+    size_t at;  // offset in b where the hole sits
+    const uint8_t* p;
+    size_t n;
+  };
   std::vector<uint8_t> b;
-  uint64_t pos() const { return b.size(); }
+  std::vector<Hole> holes;
+  uint64_t skipped = 0;
+  uint64_t pos() const { return b.size() + skipped; }
+  void hole(const uint8_t* p, size_t n) {
+    holes.push_back({b.size(), p, n});
+    skipped += n;
+  }
   void u8(uint8_t v) { b.push_back(v); }
   void u16(uint16_t v) { for (int i = 0; i < 2; ++i) b.push_back((v >> (8 * i)) & 0xff); }
   void u32(uint32_t v) { for (int i = 0; i < 4; ++i) b.push_back((v >> (8 * i)) & 0xff); }
@@ -119,7 +152,7 @@ struct Buf {
     b.insert(b.end(), c, c + n);
   }
   void zeros(size_t n) { b.insert(b.end(), n, 0); }
-  void pad8() { while (b.size() % 8) b.push_back(0); }
+  void pad8() { while (pos() % 8) b.push_back(0); }
   void put64(uint64_t at, uint64_t v) { for (int i = 0; i < 8; ++i) b[at + i] = (v >> (8 * i)) & 0xff; }
 };
 
@@ -217,16 +250,19 @@ struct Emitter {
 
   uint64_t emit_dataset(const Writer::Node& n) {
     uint64_t daddr = UNDEF;
-    if (!n.data.empty()) {
+    if (n.nbytes()) {
       B.pad8();
       daddr = B.pos();
-      B.bytes(n.data.data(), n.data.size());
+      if (n.ext)
+        B.hole(n.ext, n.ext_bytes);
+      else
+        B.bytes(n.data.data(), n.data.size());
     }
     B.pad8();
     std::vector<Msg> msgs;
     msgs.push_back(dataspace_msg(n.dims));
     msgs.push_back(datatype_msg(n.t));
-    msgs.push_back(layout_msg(daddr, n.data.size()));
+    msgs.push_back(layout_msg(daddr, n.nbytes()));
     return emit_ohdr_v1(B, msgs);
   }
 
@@ -357,10 +393,48 @@ struct Emitter {
 };
 }  // namespace
 
+namespace {
+// Metadata with holes, superblock patched.
+void emit_file(const Writer::Node& root, Buf* out);
+}  // namespace
+
 std::vector<uint8_t> Writer::serialize() const {
+  Buf B;
+  emit_file(*root_, &B);
+  std::vector<uint8_t> f;
+  f.reserve(B.pos());
+  size_t at = 0;
+  for (const auto& h : B.holes) {
+    f.insert(f.end(), B.b.begin() + at, B.b.begin() + h.at);
+    f.insert(f.end(), h.p, h.p + h.n);
+    at = h.at;
+  }
+  f.insert(f.end(), B.b.begin() + at, B.b.end());
+  return f;
+}
+
+bool Writer::write(const std::string& filename) const {
+  Buf B;
+  emit_file(*root_, &B);
+  FILE* f = std::fopen(filename.c_str(), "wb");
+  if (!f) return false;
+  bool ok = true;
+  size_t at = 0;
+  for (const auto& h : B.holes) {
+    ok = ok && std::fwrite(B.b.data() + at, 1, h.at - at, f) == h.at - at;
+    ok = ok && std::fwrite(h.p, 1, h.n, f) == h.n;
+    at = h.at;
+  }
+  ok = ok && std::fwrite(B.b.data() + at, 1, B.b.size() - at, f) == B.b.size() - at;
+  int c = std::fclose(f);
+  return ok && c == 0;
+}
+
+namespace {
+void emit_file(const Writer::Node& root, Buf* out) {
   Emitter E;
   E.B.zeros(96);
-  GroupRefs r = E.emit_group(*root_);
+  GroupRefs r = E.emit_group(root);
   E.B.pad8();
   Buf& B = E.B;
   uint64_t eof = B.pos();
@@ -378,17 +452,9 @@ std::vector<uint8_t> Writer::serialize() const {
   s[72] = 1; s[73] = 0; s[74] = 0; s[75] = 0;  // cache type 1: symbol table info cached
   B.put64(80, r.btree);
   B.put64(88, r.heap);
-  return std::move(B.b);
+  *out = std::move(B);
 }
-
-bool Writer::write(const std::string& filename) const {
-  auto bytes = serialize();
-  FILE* f = std::fopen(filename.c_str(), "wb");
-  if (!f) return false;
-  size_t w = std::fwrite(bytes.data(), 1, bytes.size(), f);
-  int c = std::fclose(f);
-  return w == bytes.size() && c == 0;
-}
+}  // namespace
 
 // =============================================================================================
 // Reader

@@ -36,6 +36,9 @@ class Writer {
   // duplicate name or a path that passes through an existing dataset.
   bool add_dataset(const std::string& path, DType t, const std::vector<uint64_t>& dims,
                    const void* data);
+  // The same without a copy: `data` must stay valid and unchanged until write()/serialize().
+  bool add_dataset_ref(const std::string& path, DType t, const std::vector<uint64_t>& dims,
+                       const void* data);
   // Serialize and write the file (truncating). Returns false on I/O error.
   bool write(const std::string& filename) const;
   std::vector<uint8_t> serialize() const;
@@ -45,6 +48,7 @@ class Writer {
  private:
   std::unique_ptr<Node> root_;
   Node* make_group(const std::string& path);
+  bool add(const std::string& path, DType t, const std::vector<uint64_t>& dims, const void* data, bool copy);
 };
 
 // ---------------------------------------------------------------------------------------------

@@ -260,11 +260,6 @@ static int validate(const pg_setup_desc* s, const pg_config* c, bool bonds_on_ho
   return PG_OK;
 }
 
-static uint32_t next_pow2(uint64_t x) {
-  uint32_t p = 1;
-  while (p < x) p <<= 1;
-  return p;
-}
 
 static int create_impl(const pg_setup_desc* s, const pg_config* cfg_in, pg_handle** out);
 

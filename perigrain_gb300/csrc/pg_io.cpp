@@ -6,6 +6,8 @@
 #include <algorithm>
 #include <cctype>
 #include <chrono>
+#include <condition_variable>
+#include <deque>
 #include <cstdlib>
 #include <cmath>
 #include <cstdio>
@@ -14,8 +16,10 @@
 #include <fstream>
 #include <iomanip>
 #include <iostream>
+#include <mutex>
 #include <sstream>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/perigrain.h"
@@ -584,20 +588,20 @@ static int write_tc(pg_setup* s, const std::string& dir, uint32_t counter, const
   char buf[64];
   std::snprintf(buf, sizeof buf, "%05u", counter);
   h5l::Writer w;
+  std::vector<std::vector<uint32_t>> conns(connectivity ? s->G : 0);  // borrowed by w until written
   for (uint32_t g = 0; g < s->G; ++g) {
     char gb[32];
     std::snprintf(gb, sizeof gb, "P_%05u/", g);
     std::string pre(gb);
     const uint32_t n0 = s->node_off[g], n = s->node_off[g + 1] - n0;
     w.create_group(pre);
-    w.add_dataset(pre + "CurrPos", h5l::DType::F64, {n, D}, cur + (size_t)n0 * D);
-    w.add_dataset(pre + "vel", h5l::DType::F64, {n, D}, vel + (size_t)n0 * D);
-    w.add_dataset(pre + "acc", h5l::DType::F64, {n, D}, acc + (size_t)n0 * D);
-    w.add_dataset(pre + "force", h5l::DType::F64, {n, D}, force + (size_t)n0 * D);
+    w.add_dataset_ref(pre + "CurrPos", h5l::DType::F64, {n, D}, cur + (size_t)n0 * D);
+    w.add_dataset_ref(pre + "vel", h5l::DType::F64, {n, D}, vel + (size_t)n0 * D);
+    w.add_dataset_ref(pre + "acc", h5l::DType::F64, {n, D}, acc + (size_t)n0 * D);
+    w.add_dataset_ref(pre + "force", h5l::DType::F64, {n, D}, force + (size_t)n0 * D);
     if (connectivity) {  // run_timeloop_worm writes none (timeloop.h:1283-1292)
-      std::vector<uint32_t> conn;
-      rows_to_conn(s, g, alive, &conn);
-      w.add_dataset(pre + "Connectivity", h5l::DType::U32, {conn.size() / 2, 2}, conn.data());
+      rows_to_conn(s, g, alive, &conns[g]);
+      w.add_dataset_ref(pre + "Connectivity", h5l::DType::U32, {conns[g].size() / 2, 2}, conns[g].data());
     }
   }
   if (!w.write(dir + "/tc_" + buf + ".h5")) return iofail(PG_EIO, "cannot write " + dir + "/tc_" + buf + ".h5");
@@ -621,6 +625,136 @@ static int snapshot(pg_handle* h, pg_setup* s, const char* out_dir, uint32_t cou
     return iofail(rc, pg_last_error());
   return write_tc(s, out_dir, counter, cur.data(), vel.data(), acc.data(), force.data(), alive.data(), wall.data(),
                   reaction.data(), connectivity);
+}
+
+// One output's buffers (page-locked: the snapshot copies land there directly) and its job.
+struct OutSet {
+  void* fields_mem = nullptr;
+  void* alive_mem = nullptr;
+  double *cur = nullptr, *vel = nullptr, *acc = nullptr, *force = nullptr;
+  uint8_t* alive = nullptr;
+  std::vector<double> wall, react;
+  uint64_t too_close = 0;
+  uint32_t counter = 0, e = 0;
+  int rc = PG_OK;
+  std::string err;
+  bool done = false;
+  std::vector<double> v, a, x, f, dmg, fs, phi;  // post-processing at the output step
+  ~OutSet() {
+    pg_host_free(fields_mem);
+    pg_host_free(alive_mem);
+  }
+};
+
+// Writer threads over a ring of OutSets: acquire() a free set, fill it, submit() it; outputs are
+// written concurrently and handed back in submission order by pop_done().
+class OutputPool {
+ public:
+  OutputPool(pg_handle* h, pg_setup* s, const std::string& dir, bool connectivity, uint32_t n_writers)
+      : h_(h), s_(s), dir_(dir), conn_(connectivity) {
+    for (uint32_t k = 0; k < n_writers; ++k) th_.emplace_back([this] { work(); });
+    if (n_writers) sets_.resize(n_writers + 1);
+  }
+  ~OutputPool() {
+    pg_wait(h_);  // a snapshot still copying into a set (an error return) completes first
+    {
+      std::lock_guard<std::mutex> lk(m_);
+      stop_ = true;
+    }
+    cv_job_.notify_all();
+    for (auto& t : th_) t.join();
+  }
+  int alloc(size_t nd, size_t n_bonds, uint32_t dim) {
+    for (auto& o : sets_) {
+      int rc = pg_host_alloc(4 * nd * sizeof(double), &o.fields_mem);
+      if (!rc) rc = pg_host_alloc(n_bonds + 1, &o.alive_mem);
+      if (rc) return rc;
+      o.cur = static_cast<double*>(o.fields_mem);
+      o.vel = o.cur + nd;
+      o.acc = o.vel + nd;
+      o.force = o.acc + nd;
+      o.alive = static_cast<uint8_t*>(o.alive_mem);
+      o.wall.assign(2 * dim, 0.0);
+      o.react.assign((size_t)2 * dim * dim, 0.0);
+      free_.push_back(&o);
+    }
+    return PG_OK;
+  }
+  // A free set, or null when every set holds an output not yet finalised.
+  OutSet* acquire() {
+    if (free_.empty()) return nullptr;
+    OutSet* o = free_.front();
+    free_.pop_front();
+    return o;
+  }
+  void submit(OutSet* o) {
+    {
+      std::lock_guard<std::mutex> lk(m_);
+      o->done = false;
+      o->rc = PG_OK;
+      o->err.clear();
+      q_.push_back(o);
+      order_.push_back(o);
+    }
+    cv_job_.notify_one();
+  }
+  // Whether the oldest submitted output is written (waiting for it when `wait`); false if none.
+  bool front_done(bool wait) {
+    std::unique_lock<std::mutex> lk(m_);
+    if (order_.empty()) return false;
+    if (wait) cv_done_.wait(lk, [this] { return order_.front()->done; });
+    return order_.front()->done;
+  }
+  // The oldest submitted output, after its files are written.
+  OutSet* pop_done() {
+    std::unique_lock<std::mutex> lk(m_);
+    cv_done_.wait(lk, [this] { return order_.front()->done; });
+    OutSet* o = order_.front();
+    order_.pop_front();
+    return o;
+  }
+  void release(OutSet* o) { free_.push_back(o); }
+
+ private:
+  void work() {
+    for (;;) {
+      OutSet* o;
+      {
+        std::unique_lock<std::mutex> lk(m_);
+        cv_job_.wait(lk, [this] { return stop_ || !q_.empty(); });
+        if (q_.empty()) return;
+        o = q_.front();
+        q_.pop_front();
+      }
+      int rc = write_tc(s_, dir_, o->counter, o->cur, o->vel, o->acc, o->force, conn_ ? o->alive : nullptr,
+                        o->wall.data(), o->react.data(), conn_);
+      {
+        std::lock_guard<std::mutex> lk(m_);
+        o->rc = rc;
+        if (rc) o->err = io_err;
+        o->done = true;
+      }
+      cv_done_.notify_all();
+    }
+  }
+  pg_handle* h_;
+  pg_setup* s_;
+  std::string dir_;
+  bool conn_;
+  std::vector<std::thread> th_;
+  std::deque<OutSet> sets_;
+  std::deque<OutSet*> free_, q_, order_;
+  std::mutex m_;
+  std::condition_variable cv_job_, cv_done_;
+  bool stop_ = false;
+};
+
+extern "C" int pg_write_tc(pg_setup* s, const char* out_dir, uint32_t counter, const double* currpos,
+                           const double* vel, const double* acc, const double* force, const uint8_t* bond_alive,
+                           const double* wall, const double* reaction, int32_t connectivity) {
+  if (!s || !out_dir || !currpos || !vel || !acc || !force || !wall || !reaction)
+    return iofail(PG_EINVAL, "null argument");
+  return write_tc(s, out_dir, counter, currpos, vel, acc, force, bond_alive, wall, reaction, connectivity != 0);
 }
 
 extern "C" int pg_write_snapshot(pg_handle* h, pg_setup* s, const char* out_dir, uint32_t counter) {
@@ -774,52 +908,40 @@ extern "C" int pg_run_simulation(const char* root_c, uint32_t dim, int32_t preci
   const uint32_t T = C.timesteps;
   uint64_t too_close_seen = 0;
 
-  // Output is pipelined: the snapshot of output step e is taken on the device (pg_snapshot) and its
-  // files are written while the GPU computes the next segment; stdout keeps the reference's order
-  // (a hook's message after the output line of the steps before it).
-  struct HostBuf {
-    void* p = nullptr;
-    ~HostBuf() { pg_host_free(p); }
-  };
+  // Output is pipelined: the snapshot of output step e is taken on the device (pg_snapshot) into
+  // one of a ring of page-locked buffer sets while the GPU runs the next segment, and its files
+  // are written by a pool of writer threads, several outputs at once (each output is its own pair
+  // of files). Progress lines are printed in output order, before a hook's message at the step
+  // after them, as the reference prints them.
   const size_t nd = (size_t)S->N * dim;
-  HostBuf hb_fields, hb_alive;
-  double *o_cur = nullptr, *o_vel = nullptr, *o_acc = nullptr, *o_force = nullptr;
-  uint8_t* o_alive = nullptr;
-  std::vector<double> o_wall(2 * dim), o_react((size_t)2 * dim * dim);
-  uint64_t o_too_close = 0;
+  const size_t set_bytes = 4 * nd * sizeof(double) + S->bond_local.size() + 1;
+  uint32_t n_writers = 0;
   if (C.save_file && C.modulo) {
-    if ((rc = pg_host_alloc(4 * nd * sizeof(double), &hb_fields.p))) return iofail(rc, pg_last_error());
-    if ((rc = pg_host_alloc(S->bond_local.size() + 1, &hb_alive.p))) return iofail(rc, pg_last_error());
-    o_cur = static_cast<double*>(hb_fields.p);
-    o_vel = o_cur + nd;
-    o_acc = o_vel + nd;
-    o_force = o_acc + nd;
-    o_alive = static_cast<uint8_t*>(hb_alive.p);
+    const char* w_env = std::getenv("PERIGRAIN_WRITERS");
+    long w = w_env && *w_env ? std::strtol(w_env, nullptr, 10) : 4;
+    w = std::max(1L, std::min(16L, w));
+    // at most ~4 GB of page-locked buffers
+    while (w > 1 && (size_t)(w + 1) * set_bytes > ((size_t)4 << 30)) --w;
+    n_writers = (uint32_t)w;
   }
-  struct Pending {
-    bool on = false;
-    uint32_t counter = 0, e = 0;
-    std::vector<double> v, a, x, f, dmg, fs, phi;  // post-processing at the output step
-  } pend;
-  auto finish_output = [&]() -> int {
-    if (!pend.on) return PG_OK;
-    pend.on = false;
-    int r = pg_wait(H);
-    if (r) return iofail(r, pg_last_error());
-    for (; too_close_seen < o_too_close; ++too_close_seen) std::cout << "Error: nodes too close" << std::endl;
-    r = write_tc(S, out, pend.counter, o_cur, o_vel, o_acc, o_force, o_alive, o_wall.data(), o_react.data(), !worm);
-    if (r) return r;
+  OutputPool pool(H, S, out, !worm, n_writers);
+  if (n_writers && (rc = pool.alloc(nd, S->bond_local.size(), dim))) return iofail(rc, pg_last_error());
+  // finalise the oldest output (its files written): messages, time series, progress line
+  auto finalize_one = [&]() -> int {
+    OutSet* o = pool.pop_done();
+    if (o->rc) return iofail(o->rc, o->err);
+    for (; too_close_seen < o->too_close; ++too_close_seen) std::cout << "Error: nodes too close" << std::endl;
     if (tsd) {
-      ts_time.push_back((double)pend.counter * C.dt * (double)C.modulo);  // extract_bulk: t * dt * modulo
-      ts_wall.insert(ts_wall.end(), o_wall.begin(), o_wall.end());
-      ts_react.insert(ts_react.end(), o_react.begin(), o_react.end());
-      ts_phi.push_back(pend.phi[0]);
-      ts_dmg.insert(ts_dmg.end(), pend.dmg.begin(), pend.dmg.end());
-      ts_force.insert(ts_force.end(), pend.f.begin(), pend.f.end());
-      ts_vel.insert(ts_vel.end(), pend.v.begin(), pend.v.end());
-      ts_acc.insert(ts_acc.end(), pend.a.begin(), pend.a.end());
-      ts_pos.insert(ts_pos.end(), pend.x.begin(), pend.x.end());
-      ts_fsum.insert(ts_fsum.end(), pend.fs.begin(), pend.fs.end());
+      ts_time.push_back((double)o->counter * C.dt * (double)C.modulo);  // extract_bulk: t * dt * modulo
+      ts_wall.insert(ts_wall.end(), o->wall.begin(), o->wall.end());
+      ts_react.insert(ts_react.end(), o->react.begin(), o->react.end());
+      ts_phi.push_back(o->phi[0]);
+      ts_dmg.insert(ts_dmg.end(), o->dmg.begin(), o->dmg.end());
+      ts_force.insert(ts_force.end(), o->f.begin(), o->f.end());
+      ts_vel.insert(ts_vel.end(), o->v.begin(), o->v.end());
+      ts_acc.insert(ts_acc.end(), o->a.begin(), o->a.end());
+      ts_pos.insert(ts_pos.end(), o->x.begin(), o->x.end());
+      ts_fsum.insert(ts_fsum.end(), o->fs.begin(), o->fs.end());
     }
     auto stop_time = std::chrono::system_clock::now();
     auto duration = std::chrono::duration_cast<std::chrono::milliseconds>(stop_time - start_time);
@@ -830,7 +952,7 @@ extern "C" int pg_run_simulation(const char* root_c, uint32_t dim, int32_t preci
       for (size_t cc = run_time.size() - avgsteps; cc < run_time.size(); ++cc) avg_duration += run_time[cc];
       avg_duration /= avgsteps;
     }
-    int rem_counts = (int)last_counter - (int)pend.counter;
+    int rem_counts = (int)last_counter - (int)o->counter;
     if (worm) {
       // the worm loop's line (timeloop.h:1331-1350): t, counter, duration/100, remaining m s, ctime
       avg_duration = 0;
@@ -839,7 +961,7 @@ extern "C" int pg_run_simulation(const char* root_c, uint32_t dim, int32_t preci
       avg_duration /= avgsteps;
       const double rem_min = (rem_counts * avg_duration) / 1e3 / 60;
       time_t now = time(NULL);
-      std::cout << pend.e << "\t" << pend.counter << "\t" << duration.count() / 100 << "\t" << (int)rem_min << "m"
+      std::cout << o->e << "\t" << o->counter << "\t" << duration.count() / 100 << "\t" << (int)rem_min << "m"
                 << (rem_min - (int)rem_min) * 60 << "s" << "\t" << ctime(&now);
     } else {
       int rem_s = (int)((rem_counts * avg_duration) / 1e3);
@@ -848,12 +970,29 @@ extern "C" int pg_run_simulation(const char* root_c, uint32_t dim, int32_t preci
       time_t now = time(NULL);
       char ts[80];
       strftime(ts, sizeof ts, "%F-%T", localtime(&now));
-      std::cout << std::left << std::setw(column_w) << pend.e << std::left << std::setw(column_w) << pend.counter
+      std::cout << std::left << std::setw(column_w) << o->e << std::left << std::setw(column_w) << o->counter
                 << std::left << std::setw(column_w) << (double)duration.count() / 1000 << std::left
                 << std::setw(column_w + 5) << rem << std::left << std::setw(column_w + 10) << ts << std::endl;
     }
     run_time.push_back((double)duration.count());
-    t_ind.push_back(pend.e);
+    t_ind.push_back(o->e);
+    pool.release(o);
+    return PG_OK;
+  };
+  OutSet* filling = nullptr;  // snapshot in flight
+  // hand the snapshot in flight to the writers (its copies done); with `all`, also wait for
+  // every output written and finalise it
+  auto flush_outputs = [&](bool all) -> int {
+    if (filling) {
+      int r = pg_wait(H);
+      if (r) return iofail(r, pg_last_error());
+      pool.submit(filling);
+      filling = nullptr;
+    }
+    while (pool.front_done(all)) {
+      int r = finalize_one();
+      if (r) return r;
+    }
     return PG_OK;
   };
 
@@ -863,7 +1002,7 @@ extern "C" int pg_run_simulation(const char* root_c, uint32_t dim, int32_t preci
     const bool hook_stoppable = !worm && C.set_stoppable_index != -1 && (uint32_t)C.set_stoppable_timestep == t;
     const bool hook_reset = !worm && C.reset_partzero_y && C.reset_partzero_y_timestep == t && S->G > 1;
     if (hook_movable || hook_stoppable || hook_reset)
-      if ((rc = finish_output())) return rc;
+      if ((rc = flush_outputs(true))) return rc;
     // hooks at the start of step t (timeloop.h:612-650); the worm loop has none
     if (hook_movable) {
       std::cout << "Setting particle " << C.set_movable_index << " to movable on timestep " << t << std::endl;
@@ -904,44 +1043,49 @@ extern "C" int pg_run_simulation(const char* root_c, uint32_t dim, int32_t preci
     if (!worm && C.reset_partzero_y) hook(C.reset_partzero_y_timestep);
     if (e < t) e = t;
     if ((rc = pg_step(H, e - t + 1))) return iofail(rc, pg_last_error());
-    // the previous output's files are written while these steps run
-    if ((rc = finish_output())) return rc;
+    // the previous output goes to the writers while these steps run
+    if ((rc = flush_outputs(false))) return rc;
     t = e + 1;
     if (C.save_file && C.modulo && (e % C.modulo) == 0) {
+      OutSet* o = pool.acquire();  // a free buffer set: may wait for the oldest output's files
+      if (!o) {
+        if ((rc = finalize_one())) return rc;
+        o = pool.acquire();
+      }
       pg_snapshot_desc sd{};
-      sd.currpos = o_cur;
-      sd.vel = o_vel;
-      sd.acc = o_acc;
-      sd.force = o_force;
-      sd.bond_alive = worm ? nullptr : o_alive;
-      sd.wall = o_wall.data();
-      sd.reaction = o_react.data();
-      sd.too_close_events = &o_too_close;
+      sd.currpos = o->cur;
+      sd.vel = o->vel;
+      sd.acc = o->acc;
+      sd.force = o->force;
+      sd.bond_alive = worm ? nullptr : o->alive;
+      sd.wall = o->wall.data();
+      sd.reaction = o->react.data();
+      sd.too_close_events = &o->too_close;
       if ((rc = pg_snapshot(H, &sd))) return iofail(rc, pg_last_error());
-      pend.on = true;
-      pend.counter = counter;
-      pend.e = e;
+      o->counter = counter;
+      o->e = e;
+      filling = o;
       if (tsd) {
         const uint32_t G = S->G;
-        pend.v.assign((size_t)G * dim, 0.0);
-        pend.a = pend.x = pend.f = pend.v;
-        pend.dmg.assign(G, 0.0);
-        pend.fs.assign(dim, 0.0);
-        pend.phi.assign(1, 0.0);
+        o->v.assign((size_t)G * dim, 0.0);
+        o->a = o->x = o->f = o->v;
+        o->dmg.assign(G, 0.0);
+        o->fs.assign(dim, 0.0);
+        o->phi.assign(1, 0.0);
         pg_post po{};
-        po.grain_mean_vel = pend.v.data();
-        po.grain_mean_acc = pend.a.data();
-        po.grain_mean_currpos = pend.x.data();
-        po.grain_force = pend.f.data();
-        po.grain_damage = pend.dmg.data();
-        po.inertial_force = pend.fs.data();
-        po.volume_fraction = pend.phi.data();
+        po.grain_mean_vel = o->v.data();
+        po.grain_mean_acc = o->a.data();
+        po.grain_mean_currpos = o->x.data();
+        po.grain_force = o->f.data();
+        po.grain_damage = o->dmg.data();
+        po.inertial_force = o->fs.data();
+        po.volume_fraction = o->phi.data();
         if ((rc = pg_postprocess(H, &po))) return iofail(rc, pg_last_error());
       }
       ++counter;
     }
   }
-  if ((rc = finish_output())) return rc;
+  if ((rc = flush_outputs(true))) return rc;
   if ((rc = pg_synchronize(H))) return iofail(rc, pg_last_error());
   {
     h5l::Writer w;

@@ -511,7 +511,7 @@ __global__ void __launch_bounds__(128) k_force_mx(const Dev P) {
       }
     }
     const uint32_t mydeg = P.node_deg[d];
-    const float Rc0 = (float)in.contact_rad, Kn0 = (float)in.normal_stiffness;
+    const float Kn0 = (float)in.normal_stiffness;
     const float mu0 = (float)in.friction_coefficient, zeta0 = (float)in.damping_ratio;
     const float rho = (float)gr.rho, dtf = (float)P.dt;
     double xp64[D];

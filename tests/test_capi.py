@@ -69,3 +69,40 @@ def test_setup_h5_roundtrip(tmp_path):
     assert list(np.ctypeslib.as_array(d.wall_geom, (4,))) == list(s.wall_geom)
     assert d.contact_radius[0] == s.contact_radius[0]
     L.pg_setup_free(h)
+
+
+def test_write_tc_from_host_arrays(tmp_path):
+    """pg_write_tc: the tc_/wall_ layout (timeloop.h:881-1006) from host arrays, Connectivity from
+    the alive bytes (i < q, rows in CSR order), datasets borrowed by the writer without a copy."""
+    from perigrain_gb300 import h5
+
+    s = setups.small_pair(dim=2, wall=True)
+    L = N.lib()
+    h = C.c_void_p()
+    d = s.desc()
+    N.check(L.pg_setup_from_desc(C.byref(d), C.byref(h)))
+    rng = np.random.default_rng(5)
+    f = [rng.standard_normal((s.n_nodes, 2)) for _ in range(4)]
+    alive = (rng.random(s.n_bonds) > 0.2).astype(np.uint8)
+    wall, re_ = rng.standard_normal(4), rng.standard_normal(8)
+    out = str(tmp_path)
+    N.check(L.pg_write_tc(h, out.encode(), 7, *[N.ptr(a, C.c_double) for a in f], N.ptr(alive, C.c_uint8),
+                          N.ptr(wall, C.c_double), N.ptr(re_, C.c_double), 1))
+    tc, wf = os.path.join(out, "tc_00007.h5"), os.path.join(out, "wall_00007.h5")
+    off = np.asarray(s.grain_node_offset, np.int64)
+    bo = np.asarray(s.bond_offset, np.int64)
+    for g in range(s.n_grains):
+        sl = slice(off[g], off[g + 1])
+        for name, a in zip(("CurrPos", "vel", "acc", "force"), f):
+            assert np.array_equal(h5.read(tc, "P_%05d/%s" % (g, name)), a[sl])
+        conn = []
+        for i in range(off[g], off[g + 1]):
+            for b in range(bo[i], bo[i + 1]):
+                q = int(s.bond_local[b])
+                if alive[b] and i - off[g] < q:
+                    conn.append([int(i - off[g]), q])
+        got = h5.read(tc, "P_%05d/Connectivity" % g, np.uint32)
+        assert got.tolist() == conn
+    assert np.array_equal(h5.read(wf, "wall_info").ravel(), wall)
+    assert np.array_equal(h5.read(wf, "reaction").ravel(), re_)
+    L.pg_setup_free(h)
