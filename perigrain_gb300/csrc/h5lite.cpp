@@ -667,13 +667,20 @@ struct Reader::Impl {
     return true;
   }
 
+  // member tables of the groups resolved so far, by object header address (the file is read-only)
+  std::map<uint64_t, std::map<std::string, uint64_t>> member_cache;
+
   bool resolve(const std::string& path, uint64_t* oh) {
     uint64_t cur = root_ohdr;
     for (auto& part : split_path(path)) {
-      std::map<std::string, uint64_t> mem;
-      if (!members(cur, &mem)) return false;
-      auto it = mem.find(part);
-      if (it == mem.end()) return fail("no such object: " + path);
+      auto c = member_cache.find(cur);
+      if (c == member_cache.end()) {
+        std::map<std::string, uint64_t> mem;
+        if (!members(cur, &mem)) return false;
+        c = member_cache.emplace(cur, std::move(mem)).first;
+      }
+      auto it = c->second.find(part);
+      if (it == c->second.end()) return fail("no such object: " + path);
       cur = it->second;
     }
     *oh = cur;
@@ -785,6 +792,7 @@ bool Reader::open(const std::string& filename) {
 
 bool Reader::open_memory(std::vector<uint8_t> bytes) {
   impl_->f = std::move(bytes);
+  impl_->member_cache.clear();
   return impl_->parse_superblock();
 }
 

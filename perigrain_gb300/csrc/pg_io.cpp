@@ -200,12 +200,19 @@ uint64_t nrows(const std::vector<uint64_t>& dims) { return dims.empty() ? 1 : di
 }  // namespace
 
 // conn2NArr (load_hdf5.h:28-38): row (i, j) appends j to NArr[i] and i to NArr[j]
-static void conn_to_rows(const uint32_t* conn, uint64_t m, uint32_t n, std::vector<std::vector<uint32_t>>* rows) {
-  rows->assign(n, {});
+// conn2NArr (load_hdf5.h:28-38) as CSR: row i lists the partners of i in the order the pairs
+// name them (for pair (i, j): j appended to row i, i to row j). off has n + 1 entries.
+static void conn_to_csr(const uint32_t* conn, uint64_t m, uint32_t n, std::vector<uint64_t>* off,
+                        std::vector<uint32_t>* col) {
+  off->assign((size_t)n + 1, 0);
+  for (uint64_t l = 0; l < 2 * m; ++l) ++(*off)[conn[l] + 1];
+  for (uint32_t i = 0; i < n; ++i) (*off)[i + 1] += (*off)[i];
+  col->resize(2 * m);
+  std::vector<uint64_t> fill(off->begin(), off->end() - 1);
   for (uint64_t l = 0; l < m; ++l) {
-    uint32_t i = conn[2 * l], j = conn[2 * l + 1];
-    (*rows)[i].push_back(j);
-    (*rows)[j].push_back(i);
+    const uint32_t i = conn[2 * l], j = conn[2 * l + 1];
+    (*col)[fill[i]++] = j;
+    (*col)[fill[j]++] = i;
   }
 }
 
@@ -272,12 +279,12 @@ extern "C" int pg_setup_load(const char* path, uint32_t dim, int32_t load_torque
     if (m && ncols(dims) != 2) return iofail(PG_EIO, pre + "Connectivity must be m x 2");
     for (auto x : u)
       if (x >= n) return iofail(PG_EIO, pre + "Connectivity index out of range");
-    std::vector<std::vector<uint32_t>> rows;
-    conn_to_rows(u.data(), m, (uint32_t)n, &rows);
-    for (uint64_t i = 0; i < n; ++i) {
-      for (auto j : rows[i]) s->bond_local.push_back(j);
-      s->bond_offset.push_back(s->bond_local.size());
-    }
+    std::vector<uint64_t> roff;
+    std::vector<uint32_t> rcol;
+    conn_to_csr(u.data(), m, (uint32_t)n, &roff, &rcol);
+    const uint64_t b0 = s->bond_local.size();
+    s->bond_local.insert(s->bond_local.end(), rcol.begin(), rcol.end());
+    for (uint64_t i = 0; i < n; ++i) s->bond_offset.push_back(b0 + roff[i + 1]);
     auto scalar = [&](const char* name, double* dst) {
       if (!need(in.f64(pre + name, &dims, &f), name) || f.empty()) return false;
       *dst = f[0];
@@ -484,14 +491,15 @@ extern "C" int pg_setup_set_connectivity(pg_setup* s, uint32_t g, const uint32_t
   const uint32_t n0 = s->node_off[g], n = s->node_off[g + 1] - n0;
   for (uint64_t k = 0; k < 2 * m; ++k)
     if (conn[k] >= n) return iofail(PG_EINVAL, "connectivity index out of range");
-  std::vector<std::vector<uint32_t>> rows;
-  conn_to_rows(conn, m, n, &rows);
+  std::vector<uint64_t> roff;
+  std::vector<uint32_t> rcol;
+  conn_to_csr(conn, m, n, &roff, &rcol);
   std::vector<uint64_t> off;
   std::vector<uint32_t> loc;
   off.push_back(0);
   for (uint32_t i = 0; i < s->N; ++i) {
     if (i >= n0 && i < n0 + n) {
-      for (auto j : rows[i - n0]) loc.push_back(j);
+      loc.insert(loc.end(), rcol.begin() + roff[i - n0], rcol.begin() + roff[i - n0 + 1]);
     } else {
       for (uint64_t b = s->bond_offset[i]; b < s->bond_offset[i + 1]; ++b) loc.push_back(s->bond_local[b]);
     }
@@ -918,7 +926,7 @@ extern "C" int pg_run_simulation(const char* root_c, uint32_t dim, int32_t preci
   uint32_t n_writers = 0;
   if (C.save_file && C.modulo) {
     const char* w_env = std::getenv("PERIGRAIN_WRITERS");
-    long w = w_env && *w_env ? std::strtol(w_env, nullptr, 10) : 4;
+    long w = w_env && *w_env ? std::strtol(w_env, nullptr, 10) : 8;
     w = std::max(1L, std::min(16L, w));
     // at most ~4 GB of page-locked buffers
     while (w > 1 && (size_t)(w + 1) * set_bytes > ((size_t)4 << 30)) --w;
