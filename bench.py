@@ -633,6 +633,7 @@ def main():
     # 100 steps run (pg_snapshot / pg_wait)
     snap_items = ("CurrPos", "vel", "acc", "force")
     bufs = e2e_sim.snapshot_buffers(snap_items)
+    t_bufs = time.perf_counter()
     snaps = 0
     done = 0
     d2h = 0
@@ -654,7 +655,8 @@ def main():
     t_wait += time.perf_counter() - td
     d2h += sum(got[f].nbytes for f in snap_items)
     e2e_s = time.perf_counter() - t0
-    e2e_parts = {"create_ms": (t_created - t0) * 1e3, "host_wait_ms": t_wait * 1e3}
+    e2e_parts = {"create_ms": (t_created - t0) * 1e3, "buffers_ms": (t_bufs - t_created) * 1e3,
+                 "host_wait_ms": t_wait * 1e3}
     e2e_sim.close()
     h2d = sum(getattr(setup, f).nbytes for f in ("pos", "vol", "disp", "vel", "acc", "extforce", "bond_offset",
                                                    "bond_local"))

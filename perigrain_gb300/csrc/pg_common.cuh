@@ -569,11 +569,7 @@ static __global__ void __launch_bounds__(256) k_keys(const Dev P) {
 // the worm loop; boundary nodes only when nl_bdry_only), sorted by the reference's visit order.
 // The bounding-box prefilter is applied per step, not here. Also records the displacement.
 template <int D>
-static __global__ void __launch_bounds__(128) k_cand_build(const Dev P) {
-  pdl_enter();
-  if (!*P.rebuild) return;
-  const uint32_t d = blockIdx.x * blockDim.x + threadIdx.x;
-  if (d >= P.N) return;
+__device__ __forceinline__ void cand_build_node(const Dev& P, uint32_t d) {
   const uint32_t lane = d & 31, chunk = d >> 5;
   constexpr uint32_t SF = (D == 2) ? 2 : 4;
   double dp[D];
@@ -640,10 +636,18 @@ static __global__ void __launch_bounds__(128) k_cand_build(const Dev P) {
   P.cand_n[d] = (uint8_t)n;
 }
 
+template <int D>
+static __global__ void __launch_bounds__(128) k_cand_build(const Dev P) {
+  pdl_enter();
+  if (!*P.rebuild) return;
+  const uint32_t d = blockIdx.x * blockDim.x + threadIdx.x;
+  if (d < P.N) cand_build_node<D>(P, d);
+}
+
 // ---------------------------------------------------------------------------------------------
-// Cooperative grid build (candidate lists): keys and counts, scan of the counts and scatter in one
-// launch of co-resident blocks separated by grid barriers, so a step without a rebuild costs one
-// idle launch here instead of four. The barrier waits are bounded: past GBAR_SPIN_LIMIT polls a
+// Cooperative grid build (candidate lists): keys and counts, scan of the counts, scatter and the
+// candidate-list rebuild in one launch of co-resident blocks separated by grid barriers, so a step
+// without a rebuild costs one idle launch here instead of five. The barrier waits are bounded: past GBAR_SPIN_LIMIT polls a
 // block records PG_ETIMEOUT and returns (the step's status then reports it).
 // ---------------------------------------------------------------------------------------------
 constexpr uint32_t GBAR_SPIN_LIMIT = 1u << 22;  // polls of ~64 ns: about 0.3 s
@@ -753,6 +757,9 @@ static __global__ void __launch_bounds__(SCAN_THREADS) k_grid_coop(const Dev P) 
   // 5. scatter
   for (uint32_t d = blockIdx.x * blockDim.x + threadIdx.x; d < P.N; d += nthr)
     P.sorted[P.cell_start[P.cell_key[d]] + P.cell_rank[d]] = d;
+  if (!grid_barrier(P, &ok)) return;
+  // 6. candidate lists
+  for (uint32_t d = blockIdx.x * blockDim.x + threadIdx.x; d < P.N; d += nthr) cand_build_node<D>(P, d);
 }
 
 // Grid build shared by both precisions: exclusive scan of the bucket counts, then scatter; with
@@ -774,8 +781,7 @@ inline void launch_grid_build(const Dev& P, cudaStream_t s, uint64_t* launches, 
     cfg.attrs = at;
     cfg.numAttrs = pdl ? 2 : 1;
     cudaLaunchKernelEx(&cfg, k_grid_coop<D>, P);
-    launch_k(k_cand_build<D>, cdiv(P.N, 128), 128, 0, s, pdl, P);
-    *launches += 2;
+    *launches += 1;
     return;
   }
   if (P.cand_q) {

@@ -127,10 +127,14 @@ class Simulation:
         shapes = {"bond_alive": ((max(1, self.setup.n_bonds),), np.uint8),
                   "wall": ((self.setup.n_instances, 2 * d), np.float64),
                   "reaction": ((self.setup.n_instances, 2 * d, d), np.float64)}
-        out = {}
-        for k in items:
-            shape, dt = shapes.get(k, ((n, d), np.float64))
-            out[k] = pinned_empty(shape, dt)
+        specs = [(k,) + shapes.get(k, ((n, d), np.float64)) for k in items]
+        sizes = [(int(np.prod(sh)) * np.dtype(dt).itemsize + 255) // 256 * 256 for _, sh, dt in specs]
+        block = pinned_empty((max(1, sum(sizes)),), np.uint8)  # one page-locked allocation for all
+        out, at = {}, 0
+        for (k, sh, dt), nb in zip(specs, sizes):
+            cnt = int(np.prod(sh))
+            out[k] = block[at: at + cnt * np.dtype(dt).itemsize].view(dt).reshape(sh)
+            at += nb
         return out
 
     def snapshot(self, items=("CurrPos", "vel", "acc", "force"), out=None):
