@@ -558,7 +558,7 @@ static __global__ void __launch_bounds__(256) k_keys(const Dev P) {
   float rf[D];
   ldf<D>(P.curf, d, rf);
   int32_t ci[3] = {0, 0, 0};
-  for (int c = 0; c < D; ++c) ci[c] = cell_coord(rf[c], in.inv_cell_f, in.dims[c]);
+  for (int c = 0; c < D; ++c) ci[c] = cell_coord(rf[c] + in.frame_off_f[c], in.inv_cell_f, in.dims[c]);
   const uint32_t key = in.table_off + ((uint32_t)ci[2] * in.dims[1] + (uint32_t)ci[1]) * in.dims[0] + (uint32_t)ci[0];
   P.cell_key[d] = key;
   P.cell_rank[d] = atomicAdd(&P.cell_count[key], 1u);
@@ -587,7 +587,7 @@ __device__ __forceinline__ void cand_build_node(const Dev& P, uint32_t d) {
     float pf[D];
     ldf<D>(P.curf, d, pf);
     int32_t cc[3] = {0, 0, 0};
-    for (int c = 0; c < D; ++c) cc[c] = cell_coord(pf[c], in.inv_cell_f, in.dims[c]);
+    for (int c = 0; c < D; ++c) cc[c] = cell_coord(pf[c] + in.frame_off_f[c], in.inv_cell_f, in.dims[c]);
     const float thr2 = in.pre_b * in.pre_b;
     unsigned long long keys[CAND_CAP];
     uint32_t idx[CAND_CAP];
@@ -695,7 +695,7 @@ static __global__ void __launch_bounds__(SCAN_THREADS) k_grid_coop(const Dev P) 
     float rf[D];
     ldf<D>(P.curf, d, rf);
     int32_t ci[3] = {0, 0, 0};
-    for (int c = 0; c < D; ++c) ci[c] = cell_coord(rf[c], in.inv_cell_f, in.dims[c]);
+    for (int c = 0; c < D; ++c) ci[c] = cell_coord(rf[c] + in.frame_off_f[c], in.inv_cell_f, in.dims[c]);
     const uint32_t key = in.table_off + ((uint32_t)ci[2] * in.dims[1] + (uint32_t)ci[1]) * in.dims[0] + (uint32_t)ci[0];
     P.cell_key[d] = key;
     P.cell_rank[d] = atomicAdd(&P.cell_count[key], 1u);

@@ -80,6 +80,12 @@ struct InstDev {
   float skin_lim2;      // candidate lists: squared displacement since the last build that forces
                         // a rebuild, (0.45 skin)^2 (the Verlet bound is skin/2; FP32 margin)
   uint32_t dims[3];     // cells per axis (dims[2] = 1 in 2D)
+  // rel_frame != 0 (mixed path with candidate lists): the FP32 position images (cur_hl, curf) are
+  // offsets from xorigin, which never moves, so the position update of a step does not depend on
+  // the grid refit of the step before; frame_off_f = xorigin - origin turns them into offsets from
+  // the grid origin for cell coordinates. Otherwise the images are offsets from origin, and 0.
+  float frame_off_f[3];
+  int32_t rel_frame;
   uint32_t table_off, table_cap;
   uint32_t node_begin, node_end, grain_begin, grain_end;
   int32_t allow_wall;
@@ -112,6 +118,7 @@ __host__ __device__ inline void fit_grid(InstDev& in, int D, const double* lo, c
   for (int a = 0; a < 3; ++a) {
     in.origin[a] = a < D ? lo[a] - 2.0 * (double)cs : 0.0;
     in.dims[a] = a < D ? n[a] : 1u;
+    in.frame_off_f[a] = (in.rel_frame && a < D) ? (float)(in.xorigin[a] - in.origin[a]) : 0.f;
   }
 }
 

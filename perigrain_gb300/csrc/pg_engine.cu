@@ -32,6 +32,8 @@ static int fail(int code, const std::string& msg) { return pg_fail(code, msg); }
 void set_vel(pg_handle* h, Dev& P, int parity) {
   P.vel_in = parity == 0 ? h->vel_a : h->vel_b;
   P.vel_out = parity == 0 ? h->vel_b : h->vel_a;
+  P.bbox = h->bbox_pp[parity];
+  P.rebuild = h->rebuild_pp[parity];
 }
 
 void enqueue_step(pg_handle* h, int parity, uint64_t* launches) {
@@ -46,11 +48,37 @@ void enqueue_step(pg_handle* h, int parity, uint64_t* launches) {
 
 // Force a rebuild of the contact candidate lists at the next step (after host writes of state).
 int request_list_rebuild(pg_handle* h) {
-  if (!h->P.rebuild) return PG_OK;
-  const uint32_t one = 1;
-  CU(cudaMemcpyAsync(h->P.rebuild, &one, 4, cudaMemcpyHostToDevice, h->stream));
+  if (!h->rebuild_pp[0]) return PG_OK;
+  static const uint32_t one = 1;
+  for (int p = 0; p < 2; ++p) CU(cudaMemcpyAsync(h->rebuild_pp[p], &one, 4, cudaMemcpyHostToDevice, h->stream));
   CU(cudaStreamSynchronize(h->stream));
   return PG_OK;
+}
+
+// GRAPH_STEPS mixed-precision steps from velocity parity `par` with each step's finalize on the
+// side stream beside the next step's position update (which reads none of what finalize writes:
+// the images are relative to the fixed frame, the grain boxes and rebuild flag are per parity);
+// the next grid build waits for both. The last step ends with its finalize on the main stream.
+static void enqueue_steps_overlapped(pg_handle* h, int par, uint64_t* n) {
+  Dev P[pg_handle::GRAPH_STEPS];
+  for (int k = 0; k < pg_handle::GRAPH_STEPS; ++k) {
+    P[k] = h->P;
+    set_vel(h, P[k], par ^ (k & 1));
+  }
+  launch_mixed_predict(P[0], h->stream, true, n);
+  for (int k = 0; k < pg_handle::GRAPH_STEPS; ++k) {
+    if (k > 0) cudaStreamWaitEvent(h->stream, h->ev_join, 0);
+    launch_mixed_body(P[k], h->L, h->stream, true, n);
+    if (k + 1 < pg_handle::GRAPH_STEPS) {
+      cudaEventRecord(h->ev_fork, h->stream);
+      cudaStreamWaitEvent(h->side, h->ev_fork, 0);
+      launch_mixed_finalize(P[k], h->side, false, n);
+      cudaEventRecord(h->ev_join, h->side);
+      launch_mixed_predict(P[k + 1], h->stream, true, n);
+    } else {
+      launch_mixed_finalize(P[k], h->stream, true, n);
+    }
+  }
 }
 
 int build_graphs(pg_handle* h) {
@@ -63,9 +91,13 @@ int build_graphs(pg_handle* h) {
     CU(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
     uint64_t n = 0;
     int p = par;
-    for (int k = 0; k < pg_handle::GRAPH_STEPS; ++k) {
-      enqueue_step(h, p, &n);
-      p ^= 1;
+    if (h->overlap) {
+      enqueue_steps_overlapped(h, par, &n);
+    } else {
+      for (int k = 0; k < pg_handle::GRAPH_STEPS; ++k) {
+        enqueue_step(h, p, &n);
+        p ^= 1;
+      }
     }
     CU(cudaStreamEndCapture(h->stream, &g));
     cudaError_t e = cudaGraphInstantiate(&h->graph[par], g, 0);
@@ -624,11 +656,14 @@ static int create_impl(const pg_setup_desc* s, const pg_config* cfg_in, pg_handl
   }
   CU(h->dalloc(&P.grain, G));
   CU(cudaMemcpy(P.grain, grains.data(), G * sizeof(GrainDev), cudaMemcpyHostToDevice));
-  CU(h->dalloc(&P.bbox, (size_t)G * 2 * D));
   {
     std::vector<unsigned long long> bb((size_t)G * 2 * D);
     for (size_t i = 0; i < bb.size(); ++i) bb[i] = ((i % (2 * D)) < D) ? ~0ull : 0ull;
-    CU(cudaMemcpy(P.bbox, bb.data(), bb.size() * 8, cudaMemcpyHostToDevice));
+    for (int p = 0; p < 2; ++p) {
+      CU(h->dalloc(&h->bbox_pp[p], (size_t)G * 2 * D));
+      CU(cudaMemcpy(h->bbox_pp[p], bb.data(), bb.size() * 8, cudaMemcpyHostToDevice));
+    }
+    P.bbox = h->bbox_pp[0];
   }
   CU(h->dalloc(&P.torque_c, (size_t)G * 3));
   CU(cudaMemset(P.torque_c, 0, (size_t)G * 3 * 8));
@@ -694,6 +729,7 @@ static int create_impl(const pg_setup_desc* s, const pg_config* cfg_in, pg_handl
     }
     in.pre_b = (float)cmin;
     in.cell_min = cmin;
+    in.rel_frame = (h->precision == PG_MIXED && cfg.contact_skin > 0) ? 1 : 0;
     const uint32_t nn = in.node_end - in.node_begin;
     in.table_cap = (uint32_t)std::max<uint64_t>(1024, (uint64_t)h->L.cells_per_node * nn);
     in.table_off = (uint32_t)table_total;
@@ -764,14 +800,21 @@ static int create_impl(const pg_setup_desc* s, const pg_config* cfg_in, pg_handl
     CU(h->dalloc(&P.cand_q, (size_t)P.n_chunks * 32 * CAND_CAP));
     CU(h->dalloc(&P.cand_n, N));
     CU(h->dalloc(&P.disp_b, (size_t)N * SF));
-    CU(h->dalloc(&P.rebuild, 1));
+    for (int p = 0; p < 2; ++p) CU(h->dalloc(&h->rebuild_pp[p], 1));
+    P.rebuild = h->rebuild_pp[0];
     CU(h->dalloc(&P.gbar, 2));
     CU(cudaMemset(P.gbar, 0, 8));
     P.coop_blocks = grid_coop_blocks(P, h->device);
     CU(cudaMemset(P.cand_n, 0, N));
     CU(cudaMemset(P.disp_b, 0, (size_t)N * SF * 4));
     const uint32_t one = 1;
-    CU(cudaMemcpy(P.rebuild, &one, 4, cudaMemcpyHostToDevice));
+    for (int p = 0; p < 2; ++p) CU(cudaMemcpy(h->rebuild_pp[p], &one, 4, cudaMemcpyHostToDevice));
+    if (h->precision == PG_MIXED) {
+      h->overlap = true;
+      CU(cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking));
+      CU(cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming));
+      CU(cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming));
+    }
   }
   CU(cudaEventCreate(&h->ev_t0));
   CU(cudaEventCreate(&h->ev_t1));

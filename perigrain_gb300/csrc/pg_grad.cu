@@ -96,10 +96,9 @@ static int restore_state(pg_handle* h, uint32_t slot) {
   h->next_t = G->ckpt_t[slot];
   // the restored state is not the one the candidate lists were built for (the results do not
   // depend on when the lists are rebuilt)
-  if (h->P.rebuild) {
-    const uint32_t one = 1;
-    CU(cudaMemcpyAsync(h->P.rebuild, &one, 4, cudaMemcpyHostToDevice, h->stream));
-  }
+  static const uint32_t one = 1;
+  for (int p = 0; p < 2; ++p)
+    if (h->rebuild_pp[p]) CU(cudaMemcpyAsync(h->rebuild_pp[p], &one, 4, cudaMemcpyHostToDevice, h->stream));
   return PG_OK;
 }
 

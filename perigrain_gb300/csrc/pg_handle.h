@@ -160,6 +160,14 @@ struct pg_handle {
   int vel_parity = 0;  // 0: current velocity in vel_a
   double* vel_a = nullptr;
   double* vel_b = nullptr;
+  // per step parity (the parity of vel_in): grain boxes and the list-rebuild flag of the step's
+  // positions, so the next step's position update can run beside this step's finalize
+  unsigned long long* bbox_pp[2] = {nullptr, nullptr};
+  uint32_t* rebuild_pp[2] = {nullptr, nullptr};
+  // the finalize of one step beside the next step's position update (graphs of the mixed path)
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  bool overlap = false;
   bool xpos_separate = false;
   std::vector<void*> allocs;
   // host copies needed for mapping
@@ -196,6 +204,9 @@ struct pg_handle {
     for (auto e : ev) cudaEventDestroy(e);
     if (ev_t0) cudaEventDestroy(ev_t0);
     if (ev_t1) cudaEventDestroy(ev_t1);
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_join) cudaEventDestroy(ev_join);
+    if (side) cudaStreamDestroy(side);
     for (void* p : allocs) cudaFree(p);
     if (xpos_separate) cudaFree(P.xpos);
     if (stream) cudaStreamDestroy(stream);

@@ -67,7 +67,7 @@ __global__ void __launch_bounds__(256) k_predict(const Dev P) {
     for (int c = 0; c < D; ++c) {
       if (!isfinite(cu[c])) ok = false;
       rf[c] = (float)(cu[c] - in.origin[c]);
-      ci[c] = cell_coord(rf[c], in.inv_cell_f, in.dims[c]);
+      ci[c] = cell_coord(rf[c] + in.frame_off_f[c], in.inv_cell_f, in.dims[c]);
     }
     if (!ok) set_status(P.status, PG_ENAN);
     if constexpr (D == 2) {
@@ -204,7 +204,7 @@ __global__ void __launch_bounds__(128) k_force(const Dev P) {
     float pf[D];
     ldf<D>(P.curf, d, pf);
     int32_t cc[3] = {0, 0, 0};
-    for (int c = 0; c < D; ++c) cc[c] = cell_coord(pf[c], in.inv_cell_f, in.dims[c]);
+    for (int c = 0; c < D; ++c) cc[c] = cell_coord(pf[c] + in.frame_off_f[c], in.inv_cell_f, in.dims[c]);
     const float thr2 = in.pre_f * in.pre_f;
     unsigned long long keys[MAX_CAND];
     uint32_t idx[MAX_CAND];

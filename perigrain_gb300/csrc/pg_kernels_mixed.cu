@@ -234,17 +234,18 @@ __global__ void __launch_bounds__(256) k_predict_mx(const Dev P) {
     for (int c = 0; c < D; ++c) cu[c] = ps[c] + dp[c];
     stv<D>(P.cur, d, cu);
     const InstDev& in = P.inst[gr.inst];
+    // images relative to the fixed frame with candidate lists (independent of the grid refit of
+    // the step before), else to this step's grid origin
+    const double* org = in.rel_frame ? in.xorigin : in.origin;
     double rel[D];
     float rf[4] = {0.f, 0.f, 0.f, 0.f};
-    int32_t ci[3] = {0, 0, 0};
     bool ok = true;
     float rh[D], rl[D];
     for (int c = 0; c < D; ++c) {
       if (((__double_as_longlong(cu[c]) >> 52) & 0x7ff) == 0x7ff) ok = false;  // inf or NaN
-      rel[c] = cu[c] - in.origin[c];
+      rel[c] = cu[c] - org[c];
       split_hl(rel[c], &rh[c], &rl[c]);
       rf[c] = rh[c];
-      ci[c] = cell_coord(rf[c], in.inv_cell_f, in.dims[c]);
     }
     if (!ok) set_status(P.status, PG_ENAN);
     if constexpr (D == 2) {
@@ -259,10 +260,10 @@ __global__ void __launch_bounds__(256) k_predict_mx(const Dev P) {
     } else {
       reinterpret_cast<float4*>(P.curf)[d] = make_float4(rf[0], rf[1], rf[2], 0.f);
     }
-    const uint32_t key = in.table_off + ((uint32_t)ci[2] * in.dims[1] + (uint32_t)ci[1]) * in.dims[0] + (uint32_t)ci[0];
     if (P.cand_q) {
       // candidate lists: keys only on rebuild steps (k_keys); rebuild once any node has moved
-      // 0.45 skin since the last build
+      // 0.45 skin since the last build. Nothing here reads the grid, which the previous step's
+      // finalize may be refitting at the same time.
       float m2 = 0.f;
       for (int c = 0; c < D; ++c) {
         double dpt;
@@ -271,6 +272,10 @@ __global__ void __launch_bounds__(256) k_predict_mx(const Dev P) {
       }
       if (m2 > in.skin_lim2) *P.rebuild = 1;
     } else {
+      int32_t ci[3] = {0, 0, 0};
+      for (int c = 0; c < D; ++c) ci[c] = cell_coord(rf[c] + in.frame_off_f[c], in.inv_cell_f, in.dims[c]);
+      const uint32_t key =
+          in.table_off + ((uint32_t)ci[2] * in.dims[1] + (uint32_t)ci[1]) * in.dims[0] + (uint32_t)ci[0];
       P.cell_key[d] = key;
       P.cell_rank[d] = atomicAdd(&P.cell_count[key], 1u);
     }
@@ -457,7 +462,7 @@ __global__ void __launch_bounds__(128) k_force_mx(const Dev P) {
     float ph[D], pl[D];
     ld_hl<D>(P.cur_hl, d, ph, pl);
     int32_t cc[3] = {0, 0, 0};
-    for (int c = 0; c < D; ++c) cc[c] = cell_coord(ph[c], in.inv_cell_f, in.dims[c]);
+    for (int c = 0; c < D; ++c) cc[c] = cell_coord(ph[c] + in.frame_off_f[c], in.inv_cell_f, in.dims[c]);
     const float thr2 = in.pre_f * in.pre_f;
     unsigned long long keys[MAX_CAND];
     uint32_t idx[MAX_CAND];
@@ -840,6 +845,49 @@ void launch_step_mixed(const Dev& P, const LaunchCfg& L, cudaStream_t s, uint64_
   } else {
     launch_mx<3>(P, L, s, launches, e0, e1, rec);
   }
+}
+
+void launch_mixed_predict(const Dev& P, cudaStream_t s, bool pdl, uint64_t* launches) {
+  if (P.dim == 2) {
+    launch_k(k_predict_mx<2>, cdiv(P.N, 256), 256, 0, s, pdl, P);
+  } else {
+    launch_k(k_predict_mx<3>, cdiv(P.N, 256), 256, 0, s, pdl, P);
+  }
+  *launches += 1;
+}
+
+template <int D>
+static void launch_mx_body(const Dev& P, const LaunchCfg& L, cudaStream_t s, bool pdl, uint64_t* launches) {
+  launch_grid_build<D>(P, s, launches, pdl);
+  if (P.enable_torque) {
+    launch_k(k_torque_center<D>, cdiv(P.G, 128), 128, 0, s, pdl, P);
+    *launches += 1;
+  }
+  const dim3 grid(cdiv(P.n_chunks * 32, L.force_block)), block(L.force_block);
+  if (P.grain_contact) {
+    launch_k(k_force_mx<D, false, true>, grid, block, 0, s, pdl, P);
+  } else {
+    launch_k(k_force_mx<D, false, false>, grid, block, 0, s, pdl, P);
+  }
+  *launches += 1;
+}
+
+void launch_mixed_body(const Dev& P, const LaunchCfg& L, cudaStream_t s, bool pdl, uint64_t* launches) {
+  if (P.dim == 2) {
+    launch_mx_body<2>(P, L, s, pdl, launches);
+  } else {
+    launch_mx_body<3>(P, L, s, pdl, launches);
+  }
+}
+
+void launch_mixed_finalize(const Dev& P, cudaStream_t s, bool pdl, uint64_t* launches) {
+  const uint32_t sm = P.wrec_smem ? FINAL_SMEM : 0;
+  if (P.dim == 2) {
+    launch_k(k_finalize<2>, finalize_blocks(P.I), FINAL_THREADS, sm, s, pdl, P);
+  } else {
+    launch_k(k_finalize<3>, finalize_blocks(P.I), FINAL_THREADS, sm, s, pdl, P);
+  }
+  *launches += 1;
 }
 
 }  // namespace pg

@@ -138,3 +138,23 @@ def test_mixed_block_size_does_not_change_results():
     for f in ("CurrPos", "vel", "acc", "force"):
         assert np.array_equal(runs[0].field(f), runs[1].field(f)), f
     assert np.array_equal(runs[0].bond_alive(), runs[1].bond_alive())
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_mixed_overlapped_graphs_equal_serial_launches(dim):
+    """The CUDA graphs run each step's finalize (wall move, grid refit, box reset) beside the next
+    step's position update; the serial launch sequence of the timed mode gives identical runs,
+    moving walls and list rebuilds included."""
+    s = setups.concat([setups.small_pair(dim=dim, seed=61 + k, wall=True, speed=35.0) for k in range(3)])
+    runs = []
+    for timed in (False, True):
+        g = Simulation(s, dt=2e-8, enable_fracture=1, precision="mixed", contact_skin=0.25)
+        g.set_timing(timed)
+        g.step(160)
+        runs.append(g)
+    a, b = runs
+    for f in ("CurrPos", "vel", "acc", "force", "disp"):
+        assert np.array_equal(a.field(f), b.field(f)), f
+    assert np.array_equal(a.bond_alive(), b.bond_alive())
+    assert np.array_equal(a.reaction(), b.reaction()) and np.array_equal(a.wall(), b.wall())
+    assert a.device_status() == b.device_status()
