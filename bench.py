@@ -9,7 +9,9 @@ all advanced together in one handle. A "step" is one time step of every instance
 
 Prints one JSON line (rank 0). `value` is the mixed-precision batched path (FP32 forces, FP64
 state), device-timed (CUDA events on the engine's stream, state resident in HBM, inputs larger
-than L2), with block size and grid density picked by the project autotuner. Beside it: the plain
+than L2), with block size and grid density picked by the project autotuner, over the workload's
+whole configured run by default (10,000 steps for the ensemble: the cost of a step grows as the
+collisions bring grains into contact). Beside it: the plain
 FP64 path on the same batch (`plain_fp64`), 256 sequential single-instance FP64 runs
 (`sequential_fp64`, timed on a sample of instances), the mixed-vs-FP64 position error after the
 same steps and the FP64 perturbation floor of these chaotic dynamics (`accuracy`). `e2e` goes
@@ -30,6 +32,8 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "node-steps/s"
+COMPARE_STEPS = 1000  # the FP64 path is timed over the first steps only (it is ~20x slower)
+ACCURACY_STEPS = 405  # horizon of the mixed-vs-FP64 position error (chaotic dynamics)
 # Algorithmic bytes of the dominant kernel (the fused bond + contact + wall + integrate kernel),
 # counting each array once per launch and treating neighbour gathers as cache-served:
 #   FP64:  per node  reads disp, xpos, cur, vel, acc, extforce (8*dim B each), vol (8), grain id
@@ -455,7 +459,9 @@ def packing_bench(nx=800, ny=500, repeats=3):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=0,
+                    help="timed steps (default: the workload's whole configured run, 10,000 steps for the "
+                         "collision ensemble)")
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--workload", type=int, default=3)
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
@@ -473,6 +479,10 @@ def main():
                     help="only warmup + steps of the engine (the command profiled under ncu)")
     a = ap.parse_args()
     a.warmup = max(3, a.warmup)
+    import perigrain_gb300.setups as _setups
+
+    if a.steps <= 0:
+        a.steps = _setups.WORKLOADS[a.workload]["steps"]
     rank, local_rank, world = dist_env()
     threads = os.cpu_count() or 1
 
@@ -553,9 +563,16 @@ def main():
             torch.cuda.synchronize()
 
     barrier()
+    # the first COMPARE_STEPS steps are timed on their own as well: the FP64 path is timed over them
+    k_cmp = min(a.steps, COMPARE_STEPS)
+    launches = 0
     with Clocks(local_rank) as clk:
-        ms = sim.step_timed(a.steps)
-    launches = sim.launch_count()
+        ms_cmp = sim.step_timed(k_cmp)
+        launches += sim.launch_count()
+        ms = ms_cmp
+        if a.steps > k_cmp:
+            ms += sim.step_timed(a.steps - k_cmp)
+            launches += sim.launch_count()
     barrier()
     ms_max = ms
     if dist:
@@ -567,41 +584,46 @@ def main():
     node_steps = setup.n_nodes * a.steps * world
     value = node_steps / (ms_max / 1e3)
 
-    # dominant kernel time: CUDA events around every k_force launch over the same number of steps
+    # dominant kernel time: CUDA events around every k_force launch, over the steps that follow
     sim.set_timing(True)
-    sim.step(a.steps)
+    sim.step(min(a.steps, 2000))
     force_ms, total_ms, nforce = sim.kernel_times()
     sim.set_timing(False)
     st, _ = sim.device_status()
     if st:
         raise RuntimeError("device status %d after the timed region" % st)
-    total_steps = a.warmup + 2 * a.steps
-    x_main = sim.field("CurrPos")
     post_line = None if (a.no_packing or rank != 0) else postprocess_bench(sim, setup)
     sim.close()
 
     plain = seq = accuracy = None
     if a.precision == "mixed" and rank == 0:
-        # the plain FP64 path on the same batch, same steps (FP64 = the reference's arithmetic)
+        # the plain FP64 path on the same batch over the same first steps (FP64 = the reference's
+        # arithmetic)
         s64 = Simulation(setup, **engine_kwargs(spec, "fp64"))
         s64.step(a.warmup)
-        ms64 = s64.step_timed(a.steps)
+        ms64 = s64.step_timed(k_cmp)
         s64.set_timing(True)
-        s64.step(a.steps)
+        s64.step(min(k_cmp, 200))
         f64_ms, t64_ms, n64 = s64.kernel_times()
-        x64 = s64.field("CurrPos")
         s64.close()
-        plain = {"value": setup.n_nodes * a.steps / (ms64 / 1e3), "unit": METRIC, "ms_per_step": ms64 / a.steps,
+        plain = {"value": setup.n_nodes * k_cmp / (ms64 / 1e3), "unit": METRIC, "ms_per_step": ms64 / k_cmp,
+                 "steps": k_cmp, "mixed_same_steps": setup.n_nodes * k_cmp / (ms_cmp / 1e3),
                  "k_force_ms": f64_ms / max(1, n64),
                  "fp64_tflops": setup.n_bonds * fp64_flops_per_bond(setup.dim) / (f64_ms / max(1, n64) / 1e3) / 1e12}
-        # chaos floor: FP64 again with one velocity component changed by one ulp
-        sp = setup.copy()
-        k = int(setup.grain_node_offset[1]) * setup.dim
-        sp.vel[k] = np.nextafter(sp.vel[k], np.inf)
-        sf = Simulation(sp, **engine_kwargs(spec, "fp64"))
-        sf.step(total_steps)
-        xf = sf.field("CurrPos")
-        sf.close()
+        # accuracy over ACCURACY_STEPS steps: mixed vs FP64, and the chaos floor (FP64 again with one
+        # velocity component changed by one ulp)
+        total_steps = ACCURACY_STEPS
+        runs = []
+        for prec, stp in (("mixed", setup), ("fp64", setup), ("fp64", None)):
+            if stp is None:
+                stp = setup.copy()
+                k = int(setup.grain_node_offset[1]) * setup.dim
+                stp.vel[k] = np.nextafter(stp.vel[k], np.inf)
+            r = Simulation(stp, **engine_kwargs(spec, prec))
+            r.step(total_steps)
+            runs.append(r.field("CurrPos"))
+            r.close()
+        x_main, x64, xf = runs
         scale = np.abs(x64).max()
         accuracy = {"steps": total_steps, "pos_rel_err_mixed_vs_fp64": float(np.abs(x_main - x64).max() / scale),
                     "fp64_one_ulp_perturbation_floor": float(np.abs(xf - x64).max() / scale),
@@ -610,23 +632,24 @@ def main():
                             "component moved by one ulp"}
         # 256 sequential single-instance FP64 runs, timed on a sample of instances
         ns = min(8, setup.n_instances)
+        k_seq = min(a.steps, 200)
         t_seq, nodes_seq = 0.0, 0
         for i in range(ns):
             one = instance_subset(setup, i, 1)
             si = Simulation(one, **engine_kwargs(spec, "fp64"))
             si.step(a.warmup)
-            t_seq += si.step_timed(a.steps)
+            t_seq += si.step_timed(k_seq)
             nodes_seq += one.n_nodes
             si.close()
-        seq = {"value": nodes_seq * a.steps / (t_seq / 1e3), "unit": METRIC,
-               "sample": "%d instances run one after another, %d steps each" % (ns, a.steps),
-               "est_ms_for_all_instances_per_step": t_seq / a.steps * setup.n_instances / ns}
+        seq = {"value": nodes_seq * k_seq / (t_seq / 1e3), "unit": METRIC,
+               "sample": "%d instances run one after another, %d steps each" % (ns, k_seq),
+               "est_ms_for_all_instances_per_step": t_seq / k_seq * setup.n_instances / ns}
 
     # end to end through the C ABI from host buffers
     # a run of at least 1000 steps (config 3 runs 10,000), so that creation is amortised as in use
     e2e_steps = max(a.steps, 1000)
     t0 = time.perf_counter()
-    e2e_sim = Simulation(setup, **kw)
+    e2e_sim = Simulation(setup, **kw, **tuned)  # the launch configuration the autotuner picked
     t_created = time.perf_counter()
     # a tc_ snapshot (CurrPos, vel, acc, force) every 100 steps, as the drop-in writes them: each is
     # gathered on the device behind its steps and copied to page-locked host buffers while the next
@@ -682,6 +705,8 @@ def main():
         "config": {"workload": spec["name"], "precision": a.precision, "instances": setup.n_instances,
                    "nodes": setup.n_nodes, "bonds": setup.n_bonds, "dim": D, "dt": spec["dt"],
                    "parallelism": "instances per GPU" if world == 1 else "dp%d (independent ensembles)" % world,
+                   "timed_steps": "steps %d..%d of the run (the workload's configured run is %d steps)"
+                                  % (a.warmup + 1, a.warmup + a.steps, spec["steps"]),
                    "l2": "inputs larger than L2 (%.0f MB of node and bond arrays resident)"
                          % ((alg_bytes + setup.n_bonds * 4) / 1e6)},
         "roofline": {"bound": "hbm", "kernel": "k_force" if a.precision == "fp64" else "k_force_mx",
