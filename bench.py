@@ -130,6 +130,20 @@ def dist_env():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0")), ws
 
 
+def reduce_over_ranks(dist, ms, n_nodes, device):
+    """The job's timed milliseconds (max over ranks) and nodes (sum over ranks: every rank runs its
+    own ensemble, so node counts differ); one process per GPU under torchrun."""
+    if not dist:
+        return ms, n_nodes
+    import torch
+
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    n = torch.tensor([float(n_nodes)], dtype=torch.float64, device=device)
+    dist.all_reduce(n, op=dist.ReduceOp.SUM)
+    return float(t.item()), int(round(n.item()))
+
+
 def build_workload(k, rank):
     from perigrain_gb300 import setups
 
@@ -574,14 +588,8 @@ def main():
             ms += sim.step_timed(a.steps - k_cmp)
             launches += sim.launch_count()
     barrier()
-    ms_max = ms
-    if dist:
-        import torch
-
-        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_max = float(t.item())
-    node_steps = setup.n_nodes * a.steps * world
+    ms_max, job_nodes = reduce_over_ranks(dist, ms, setup.n_nodes, "cuda")
+    node_steps = job_nodes * a.steps
     value = node_steps / (ms_max / 1e3)
 
     # dominant kernel time: CUDA events around every k_force launch, over the steps that follow
@@ -648,6 +656,7 @@ def main():
     # end to end through the C ABI from host buffers
     # a run of at least 1000 steps (config 3 runs 10,000), so that creation is amortised as in use
     e2e_steps = max(a.steps, 1000)
+    barrier()
     t0 = time.perf_counter()
     e2e_sim = Simulation(setup, **kw, **tuned)  # the launch configuration the autotuner picked
     t_created = time.perf_counter()
@@ -683,6 +692,7 @@ def main():
     e2e_sim.close()
     h2d = sum(getattr(setup, f).nbytes for f in ("pos", "vol", "disp", "vel", "acc", "extforce", "bond_offset",
                                                    "bond_local"))
+    e2e_ms, e2e_nodes = reduce_over_ranks(dist, e2e_s * 1e3, setup.n_nodes, "cuda")
 
     if rank != 0:
         return
@@ -704,6 +714,7 @@ def main():
         "dtype": "f64" if a.precision == "fp64" else "f32-forces/f64-state", "data": "synthetic (seeded generator)",
         "config": {"workload": spec["name"], "precision": a.precision, "instances": setup.n_instances,
                    "nodes": setup.n_nodes, "bonds": setup.n_bonds, "dim": D, "dt": spec["dt"],
+                   "nodes_all_ranks": job_nodes,
                    "parallelism": "instances per GPU" if world == 1 else "dp%d (independent ensembles)" % world,
                    "timed_steps": "steps %d..%d of the run (the workload's configured run is %d steps)"
                                   % (a.warmup + 1, a.warmup + a.steps, spec["steps"]),
@@ -719,7 +730,7 @@ def main():
                          "sample": "%d instances x %d steps of %s (%d nodes), reference-structured oracle port, "
                                    "%.1f s" % (cpu_info["instances"], cpu_info["steps"], spec["name"],
                                                cpu_info["nodes"], cpu_info["seconds"])},
-        "e2e": {"value": setup.n_nodes * e2e_steps / e2e_s, "unit": METRIC, "steps": e2e_steps,
+        "e2e": {"value": e2e_nodes * e2e_steps / (e2e_ms / 1e3), "unit": METRIC, "steps": e2e_steps,
                 "h2d_bytes_per_step": h2d / e2e_steps, "d2h_bytes_per_step": d2h / e2e_steps,
                 "note": "pg_create from host arrays + %d steps + %d tc_ snapshots (one every 100 steps, copied to "
                         "page-locked host buffers while the next steps run)"
