@@ -110,10 +110,8 @@ static int read_status(pg_handle* h, int32_t* st) {
 
 // one engine step with mask recording into (off, cnt, wall) of this step and the shared entry list
 // (and, when x is set, the step's tape: CurrPos, velocity, walls, step number)
-static void enqueue_rec_step(pg_handle* h, int parity, uint32_t* off, uint8_t* cnt, uint32_t* wall, uint32_t* ent,
-                             uint32_t* ent_n, uint64_t cap, uint64_t* launches, double* x = nullptr,
-                             double* v = nullptr, double* w = nullptr, uint32_t* tstep = nullptr,
-                             float* df = nullptr) {
+static Dev rec_dev(pg_handle* h, int parity, uint32_t* off, uint8_t* cnt, uint32_t* wall, uint32_t* ent,
+                   uint32_t* ent_n, uint64_t cap, double* x, double* v, double* w, uint32_t* tstep, float* df) {
   Dev P = h->P;
   set_vel(h, P, parity);
   P.rec_off = off;
@@ -127,6 +125,14 @@ static void enqueue_rec_step(pg_handle* h, int parity, uint32_t* off, uint8_t* c
   P.rec_w = w;
   P.rec_t = tstep;
   P.rec_df = df;
+  return P;
+}
+
+static void enqueue_rec_step(pg_handle* h, int parity, uint32_t* off, uint8_t* cnt, uint32_t* wall, uint32_t* ent,
+                             uint32_t* ent_n, uint64_t cap, uint64_t* launches, double* x = nullptr,
+                             double* v = nullptr, double* w = nullptr, uint32_t* tstep = nullptr,
+                             float* df = nullptr) {
+  const Dev P = rec_dev(h, parity, off, cnt, wall, ent, ent_n, cap, x, v, w, tstep, df);
   if (h->precision == PG_MIXED) {
     launch_step_mixed(P, h->L, h->stream, launches, nullptr, nullptr, true);
   } else {
@@ -218,6 +224,26 @@ static int enqueue_recompute(pg_handle* h, int parity, uint32_t len, uint32_t fi
       const double* vin = parity == 0 ? h->vel_a : h->vel_b;
       CU(cudaMemcpyAsync(X, h->P.cur, N * S * 8, cudaMemcpyDeviceToDevice, h->stream));
       CU(cudaMemcpyAsync(V, vin, N * S * 8, cudaMemcpyDeviceToDevice, h->stream));
+    } else if (h->overlap) {
+      // the recording steps with each finalize beside the next position update, as in the
+      // forward graphs (bit-identical to the serial order)
+      float* DF = G->DF ? G->DF + (size_t)i * N * (h->dim == 2 ? 4 : 6) : nullptr;
+      const Dev P = rec_dev(h, parity, G->off + (size_t)i * N, G->cnt + (size_t)i * N, G->wall + (size_t)i * N,
+                            G->ent, G->ent_n, G->ent_cap, X, V, W, G->tstep + i, DF);
+      if (i == 0) launch_mixed_predict(P, h->stream, true, launches);
+      if (i > 0) cudaStreamWaitEvent(h->stream, h->ev_join, 0);
+      launch_mixed_body(P, h->L, h->stream, true, launches, true);
+      if (i + 1 < len) {
+        cudaEventRecord(h->ev_fork, h->stream);
+        cudaStreamWaitEvent(h->side, h->ev_fork, 0);
+        launch_mixed_finalize(P, h->side, false, launches);
+        cudaEventRecord(h->ev_join, h->side);
+        Dev Pn = h->P;
+        set_vel(h, Pn, parity ^ 1);
+        launch_mixed_predict(Pn, h->stream, true, launches);
+      } else {
+        launch_mixed_finalize(P, h->stream, true, launches);
+      }
     } else {
       // the recording force kernel writes the tape itself
       float* DF = G->DF ? G->DF + (size_t)i * N * (h->dim == 2 ? 4 : 6) : nullptr;

@@ -857,7 +857,8 @@ void launch_mixed_predict(const Dev& P, cudaStream_t s, bool pdl, uint64_t* laun
 }
 
 template <int D>
-static void launch_mx_body(const Dev& P, const LaunchCfg& L, cudaStream_t s, bool pdl, uint64_t* launches) {
+static void launch_mx_body(const Dev& P, const LaunchCfg& L, cudaStream_t s, bool pdl, uint64_t* launches,
+                           bool rec) {
   launch_grid_build<D>(P, s, launches, pdl);
   if (P.enable_torque) {
     launch_k(k_torque_center<D>, cdiv(P.G, 128), 128, 0, s, pdl, P);
@@ -865,18 +866,20 @@ static void launch_mx_body(const Dev& P, const LaunchCfg& L, cudaStream_t s, boo
   }
   const dim3 grid(cdiv(P.n_chunks * 32, L.force_block)), block(L.force_block);
   if (P.grain_contact) {
-    launch_k(k_force_mx<D, false, true>, grid, block, 0, s, pdl, P);
+    if (rec) launch_k(k_force_mx<D, true, true>, grid, block, 0, s, pdl, P);
+    else launch_k(k_force_mx<D, false, true>, grid, block, 0, s, pdl, P);
   } else {
-    launch_k(k_force_mx<D, false, false>, grid, block, 0, s, pdl, P);
+    if (rec) launch_k(k_force_mx<D, true, false>, grid, block, 0, s, pdl, P);
+    else launch_k(k_force_mx<D, false, false>, grid, block, 0, s, pdl, P);
   }
   *launches += 1;
 }
 
-void launch_mixed_body(const Dev& P, const LaunchCfg& L, cudaStream_t s, bool pdl, uint64_t* launches) {
+void launch_mixed_body(const Dev& P, const LaunchCfg& L, cudaStream_t s, bool pdl, uint64_t* launches, bool rec) {
   if (P.dim == 2) {
-    launch_mx_body<2>(P, L, s, pdl, launches);
+    launch_mx_body<2>(P, L, s, pdl, launches, rec);
   } else {
-    launch_mx_body<3>(P, L, s, pdl, launches);
+    launch_mx_body<3>(P, L, s, pdl, launches, rec);
   }
 }
 

@@ -17,7 +17,8 @@ void launch_step_mixed(const Dev& P, const LaunchCfg& L, cudaStream_t s, uint64_
 // The same step in three parts (position update; grid build and force kernel; finalize), for
 // graphs that run one step's finalize beside the next step's position update.
 void launch_mixed_predict(const Dev& P, cudaStream_t s, bool pdl, uint64_t* launches);
-void launch_mixed_body(const Dev& P, const LaunchCfg& L, cudaStream_t s, bool pdl, uint64_t* launches);
+void launch_mixed_body(const Dev& P, const LaunchCfg& L, cudaStream_t s, bool pdl, uint64_t* launches,
+                       bool rec = false);
 void launch_mixed_finalize(const Dev& P, cudaStream_t s, bool pdl, uint64_t* launches);
 
 }  // namespace pg
