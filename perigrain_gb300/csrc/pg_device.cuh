@@ -167,7 +167,6 @@ struct Dev {
   // grains / instances
   GrainDev* grain;
   unsigned long long* bbox;  // [G][2*dim] ordered keys: min..., max...
-  unsigned long long* ibox;  // [I][2*dim] same, per instance (grid refit in k_finalize)
   double* torque_c;          // [G][3] centroid for torque
   InstDev* inst;
   double* reaction;          // [I][2*dim][dim]

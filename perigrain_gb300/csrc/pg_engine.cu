@@ -740,12 +740,6 @@ static int create_impl(const pg_setup_desc* s, const pg_config* cfg_in, pg_handl
   P.table_total = (uint32_t)table_total;
   CU(h->dalloc(&P.inst, I));
   CU(cudaMemcpy(P.inst, h->inst_host.data(), I * sizeof(InstDev), cudaMemcpyHostToDevice));
-  CU(h->dalloc(&P.ibox, (size_t)I * 2 * D));
-  {
-    std::vector<unsigned long long> bb((size_t)I * 2 * D);
-    for (size_t i = 0; i < bb.size(); ++i) bb[i] = ((i % (2 * D)) < D) ? ~0ull : 0ull;
-    CU(cudaMemcpy(P.ibox, bb.data(), bb.size() * 8, cudaMemcpyHostToDevice));
-  }
   CU(h->dalloc(&P.reaction, (size_t)I * 2 * D * D));
   CU(cudaMemset(P.reaction, 0, (size_t)I * 2 * D * D * 8));
 
