@@ -166,7 +166,7 @@ struct Dev {
   uint32_t* break_step;
   // grains / instances
   GrainDev* grain;
-  unsigned long long* bbox;  // [G][2*dim] ordered keys: min..., max...
+  unsigned long long* bbox;  // [G][2*dim] ordered keys: min..., max... (the step parity's buffer)
   double* torque_c;          // [G][3] centroid for torque
   InstDev* inst;
   double* reaction;          // [I][2*dim][dim]
@@ -196,7 +196,7 @@ struct Dev {
   uint32_t* cand_q;
   uint8_t* cand_n;
   float* disp_b;
-  uint32_t* rebuild;
+  uint32_t* rebuild;  // the step parity's flag (set by its position update, cleared by its finalize)
   uint32_t cand_cap;
   int32_t worm;           // run_timeloop_worm semantics (pg_config::timeloop == 1)
   // mask recording (force kernels instantiated with REC = true): per node of this step the
