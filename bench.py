@@ -53,6 +53,15 @@ def bond_bytes(precision="fp64"):
     return 12.125 if precision == "fp64" else 4.125
 
 
+def survey_bytes(n_nodes, n_bonds, dim, precision="fp64"):
+    """Algorithmic bytes of one step by the scope table's per-unit figure: per node
+    B = B_node + 12.125 deg + 16 (node stream, bond stream of index + xi_norm + alive bit, contact
+    search), B_node = (8 dim + 1) 8 for FP64 and 52 dim + 4 for mixed; summed over the nodes
+    (sum of deg = directed bonds)."""
+    b_node = (8 * dim + 1) * 8 if precision == "fp64" else 52 * dim + 4
+    return n_nodes * (b_node + 16) + n_bonds * 12.125
+
+
 def fp64_flops_per_bond(dim):
     # (dj - di) + (xj - xi): 3*dim, |e|^2: 2*dim-1, sqrt 1, stretch 2, scale 2, unit*scale+acc: 3*dim
     return 3 * dim + (2 * dim - 1) + 1 + 2 + 2 + 3 * dim
@@ -699,8 +708,13 @@ def main():
     D = setup.dim
     peak, peak_kind = load_peaks()
     force_launch_ms = force_ms / max(1, nforce)
+    # achieved: the scope table's per-unit bytes x the nodes one launch of the dominant kernel
+    # processes / its average launch time; beside it the kernel's own stream (what it must read and
+    # write with xi recomputed from the reference positions), which the DRAM traffic is compared to
+    step_bytes = survey_bytes(setup.n_nodes, setup.n_bonds, D, a.precision)
+    achieved = step_bytes / (force_launch_ms / 1e3) / 1e9
     alg_bytes = setup.n_nodes * node_bytes(D, a.precision) + setup.n_bonds * bond_bytes(a.precision)
-    achieved = alg_bytes / (force_launch_ms / 1e3) / 1e9
+    achieved_kernel = alg_bytes / (force_launch_ms / 1e3) / 1e9
     fp64_tflops = setup.n_bonds * fp64_flops_per_bond(D) / (force_launch_ms / 1e3) / 1e12
     traffic = profiled_traffic("%s/%s" % (spec["name"], a.precision))
     cpu_v, cpu_info = cpu_reference(setup, spec, a.cpu_steps, threads)
@@ -723,7 +737,16 @@ def main():
         "roofline": {"bound": "hbm", "kernel": "k_force" if a.precision == "fp64" else "k_force_mx",
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
-                     "algorithmic_bytes_per_launch": alg_bytes, "launch_ms": force_launch_ms,
+                     "algorithmic_bytes_per_launch": step_bytes,
+                     "bytes_model": "per node-step B = B_node + 12.125 deg + 16, B_node = %s"
+                                    % ("(8 dim + 1) 8" if a.precision == "fp64" else "52 dim + 4"),
+                     "kernel_stream": {"bytes_per_launch": alg_bytes, "achieved": achieved_kernel,
+                                       "frac": achieved_kernel / peak,
+                                       "model": "per node %s B, per directed bond %s B (xi from the reference "
+                                                "positions, no xi_norm stream)"
+                                                % ("72 dim + 16" if a.precision == "fp64" else "56 dim + 4",
+                                                   bond_bytes(a.precision))},
+                     "launch_ms": force_launch_ms,
                      "share_of_step": force_ms / total_ms if total_ms else None,
                      **({"fp64_tflops": fp64_tflops, "fp64_nominal_tflops": 1.25} if a.precision == "fp64" else {})},
         "cpu_baseline": {"value": cpu_v, "unit": METRIC, "cores": cpu_info["cores"], "kind": cpu_info["kind"],
