@@ -240,12 +240,20 @@ int pg_snapshot(pg_handle* h, const pg_snapshot_desc* d) {
     s.out.push_back({dst, b, bytes});
     return cudaMemcpyAsync(b, src, bytes, cudaMemcpyDeviceToHost, s.copy);
   };
+  cudaError_t e = cudaSuccess;
   if (field_bytes)
-    for (int f = 0; f < nf; ++f)
-      CU(copy_out(req[f].dst, reinterpret_cast<const char*>(a.dst[f]), field_bytes, page_locked(req[f].dst)));
-  if (want_alive) CU(copy_out(d->bond_alive, reinterpret_cast<const char*>(alive_stage), n_bonds, alive_direct));
-  CU(cudaMemcpyAsync(s.small_host, s.small_dev, s.small_bytes, cudaMemcpyDeviceToHost, s.copy));
-  CU(cudaEventRecord(s.copied, s.copy));
+    for (int f = 0; f < nf && e == cudaSuccess; ++f)
+      e = copy_out(req[f].dst, reinterpret_cast<const char*>(a.dst[f]), field_bytes, page_locked(req[f].dst));
+  if (want_alive && e == cudaSuccess)
+    e = copy_out(d->bond_alive, reinterpret_cast<const char*>(alive_stage), n_bonds, alive_direct);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(s.small_host, s.small_dev, s.small_bytes, cudaMemcpyDeviceToHost, s.copy);
+  if (e == cudaSuccess) e = cudaEventRecord(s.copied, s.copy);
+  if (e != cudaSuccess) {
+    // copies already issued into the caller's buffers finish before the error returns
+    cudaStreamSynchronize(s.copy);
+    s.out.clear();
+    CU(e);
+  }
   s.d = *d;
   s.last_step = h->next_t - 1;
   s.pending = true;
