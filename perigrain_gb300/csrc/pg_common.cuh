@@ -274,11 +274,27 @@ static __global__ void __launch_bounds__(SCAN_THREADS) k_scan_final(const Dev P)
   if (tile == gridDim.x - 1 && threadIdx.x == blockDim.x - 1) P.cell_start[P.table_total] = P.N;
 }
 
+// Node d's entry of the cell-sorted order (and, with candidate lists, its position image and key).
+__device__ __forceinline__ void scatter_node(const Dev& P, uint32_t d) {
+  const uint32_t at = P.cell_start[P.cell_key[d]] + P.cell_rank[d];
+  P.sorted[at] = d;
+  if (P.sorted_key) {
+    const uint32_t g = P.node_grain[d];
+    const uint32_t sub = P.nl_bdry_only ? P.bdry_rank[d] : (d - P.grain[g].node_begin);
+    P.sorted_key[at] = ((unsigned long long)g << 32) | sub;
+    if (P.dim == 2) {
+      reinterpret_cast<float2*>(P.sorted_pos)[at] = reinterpret_cast<const float2*>(P.curf)[d];
+    } else {
+      reinterpret_cast<float4*>(P.sorted_pos)[at] = reinterpret_cast<const float4*>(P.curf)[d];
+    }
+  }
+}
+
 static __global__ void __launch_bounds__(256) k_scatter(const Dev P) {
   pdl_enter();
   if (grid_idle(P)) return;
   const uint32_t d = blockIdx.x * blockDim.x + threadIdx.x;
-  if (d < P.N) P.sorted[P.cell_start[P.cell_key[d]] + P.cell_rank[d]] = d;
+  if (d < P.N) scatter_node(P, d);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -599,23 +615,23 @@ __device__ __forceinline__ void cand_build_node(const Dev& P, uint32_t d) {
         const uint32_t row = in.table_off + ((uint32_t)z * in.dims[1] + (uint32_t)y) * in.dims[0];
         const uint32_t b0 = P.cell_start[row + x0], b1 = P.cell_start[row + x1 + 1];
         for (uint32_t b = b0; b < b1; ++b) {
+          // the cell's entries are consecutive: index, position image and key without gathers
           const uint32_t q = P.sorted[b];
-          if (q == d) continue;
           float qf[D];
-          ldf<D>(P.curf, q, qf);
+          ldf<D>(P.sorted_pos, b, qf);
+          const unsigned long long qk = P.sorted_key[b];
+          if (q == d) continue;
           float d2 = 0.f;
           for (int c = 0; c < D; ++c) {
             const float dd = qf[c] - pf[c];
             d2 += dd * dd;
           }
           if (d2 > thr2) continue;
-          const uint32_t gq = P.node_grain[q];
+          const uint32_t gq = (uint32_t)(qk >> 32), sub = (uint32_t)qk;
           const bool same = gq == g;
           if (same ? !selfc : !other) continue;
-          if (P.nl_bdry_only && P.bdry_rank[q] == NONE) continue;
-          const uint32_t sub = P.nl_bdry_only ? P.bdry_rank[q] : (q - P.grain[gq].node_begin);
-          const unsigned long long key =
-              ((unsigned long long)(same ? 0u : 1u) << 63) | ((unsigned long long)gq << 32) | sub;
+          if (P.nl_bdry_only && sub == NONE) continue;
+          const unsigned long long key = ((unsigned long long)(same ? 0u : 1u) << 63) | qk;
           if (n >= P.cand_cap) {
             set_status(P.status, PG_ECAPACITY);
             continue;
@@ -755,8 +771,7 @@ static __global__ void __launch_bounds__(SCAN_THREADS) k_grid_coop(const Dev P) 
   if (blockIdx.x == 0 && threadIdx.x == 0) P.cell_start[P.table_total] = P.N;
   if (!grid_barrier(P, &ok)) return;
   // 5. scatter
-  for (uint32_t d = blockIdx.x * blockDim.x + threadIdx.x; d < P.N; d += nthr)
-    P.sorted[P.cell_start[P.cell_key[d]] + P.cell_rank[d]] = d;
+  for (uint32_t d = blockIdx.x * blockDim.x + threadIdx.x; d < P.N; d += nthr) scatter_node(P, d);
   if (!grid_barrier(P, &ok)) return;
   // 6. candidate lists
   for (uint32_t d = blockIdx.x * blockDim.x + threadIdx.x; d < P.N; d += nthr) cand_build_node<D>(P, d);

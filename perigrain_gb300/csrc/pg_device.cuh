@@ -154,6 +154,11 @@ struct Dev {
   uint8_t *clamped, *clamp_pending;
   // grid
   uint32_t *cell_key, *cell_rank, *cell_count, *cell_start, *sorted;
+  // with candidate lists, beside `sorted`: each entry's FP32 position image (curf layout) and
+  // candidate key (grain << 32 | rank in the reference's loop order, NONE for a node outside the
+  // nonlocal boundary when nl_bdry_only), so a list rebuild reads a cell's nodes contiguously
+  float* sorted_pos;
+  unsigned long long* sorted_key;
   uint32_t *scan_tile_sum;
   uint32_t *scan_done;
   uint32_t* gbar;      // [2] grid barrier of the cooperative grid build: arrivals, generation

@@ -794,6 +794,8 @@ static int create_impl(const pg_setup_desc* s, const pg_config* cfg_in, pg_handl
     CU(h->dalloc(&P.cand_q, (size_t)P.n_chunks * 32 * CAND_CAP));
     CU(h->dalloc(&P.cand_n, N));
     CU(h->dalloc(&P.disp_b, (size_t)N * SF));
+    CU(h->dalloc(&P.sorted_pos, (size_t)N * SF));
+    CU(h->dalloc(&P.sorted_key, N));
     for (int p = 0; p < 2; ++p) CU(h->dalloc(&h->rebuild_pp[p], 1));
     P.rebuild = h->rebuild_pp[0];
     CU(h->dalloc(&P.gbar, 2));
