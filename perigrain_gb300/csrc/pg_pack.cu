@@ -278,7 +278,10 @@ __device__ __forceinline__ double mm_ascent(const MaxiMin& M, double* px, double
   double x = clampd(0.0, M.lo[0], M.hi[0]), y = clampd(0.0, M.lo[1], M.hi[1]);
   double fx = mm_value(M, x, y);
   double step = 0.25;
-  for (int it = 0; it < 6000 && step > 1e-13; ++it) {
+  // the ascent only has to bring the point within reach of the exact solve, which takes the
+  // constraints within max(1e-6, 8 step) of the minimum; stopping at step 1e-7 (instead of running
+  // to 1e-13) halves the iterations and leaves every solved circle unchanged on the test meshes
+  for (int it = 0; it < 6000 && step > 1e-7; ++it) {
     // gradients of the constraints within `step` of the minimum: moving by step / 2 along the
     // min-norm direction of their hull raises all of them, and no other one can drop below fx
     int n = 0;
