@@ -53,7 +53,7 @@ def bond_bytes(precision="fp64"):
     return 12.125 if precision == "fp64" else 4.125
 
 
-def survey_bytes(n_nodes, n_bonds, dim, precision="fp64"):
+def node_step_bytes(n_nodes, n_bonds, dim, precision="fp64"):
     """Algorithmic bytes of one step by the scope table's per-unit figure: per node
     B = B_node + 12.125 deg + 16 (node stream, bond stream of index + xi_norm + alive bit, contact
     search), B_node = (8 dim + 1) 8 for FP64 and 52 dim + 4 for mixed; summed over the nodes
@@ -711,7 +711,7 @@ def main():
     # achieved: the scope table's per-unit bytes x the nodes one launch of the dominant kernel
     # processes / its average launch time; beside it the kernel's own stream (what it must read and
     # write with xi recomputed from the reference positions), which the DRAM traffic is compared to
-    step_bytes = survey_bytes(setup.n_nodes, setup.n_bonds, D, a.precision)
+    step_bytes = node_step_bytes(setup.n_nodes, setup.n_bonds, D, a.precision)
     achieved = step_bytes / (force_launch_ms / 1e3) / 1e9
     alg_bytes = setup.n_nodes * node_bytes(D, a.precision) + setup.n_bonds * bond_bytes(a.precision)
     achieved_kernel = alg_bytes / (force_launch_ms / 1e3) / 1e9
