@@ -880,6 +880,26 @@ bool Reader::read(const std::string& path, DType want, std::vector<uint64_t>* di
     src = &impl_->f[d.data_addr];
   }
   size_t osz = dtype_size(want);
+  // fast paths (same results as the element loop below): little-endian data already in the wanted
+  // representation is copied; signed 64-bit integers (h5py's default) to uint32 clamp in one loop
+  const bool want_float = want == DType::F64 || want == DType::F32;
+  const bool want_signed = want == DType::I32 || want == DType::I64;
+  if (!d.big_endian && es == osz &&
+      (d.type_class == 1 ? want_float : (!want_float && want_signed == d.is_signed))) {
+    out->assign(src, src + n * es);
+    return true;
+  }
+  if (!d.big_endian && d.type_class == 0 && d.is_signed && es == 8 && want == DType::U32) {
+    out->assign(n * 4, 0);
+    uint32_t* o = reinterpret_cast<uint32_t*>(out->data());
+    for (uint64_t i = 0; i < n; ++i) {
+      int64_t sv;
+      std::memcpy(&sv, src + i * 8, 8);
+      const uint32_t v = sv < 0 ? 0u : clamp_from_u<uint32_t>((uint64_t)sv);
+      std::memcpy(o + i, &v, 4);
+    }
+    return true;
+  }
   out->assign(n * osz, 0);
   for (uint64_t i = 0; i < n; ++i) {
     uint8_t e[8];
