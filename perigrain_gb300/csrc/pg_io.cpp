@@ -512,17 +512,20 @@ extern "C" int pg_setup_set_connectivity(pg_setup* s, uint32_t g, const uint32_t
 
 // NbdArr2conn (timeloop.h:25-49): rows (i, q) for i < q in row order
 static void rows_to_conn(const pg_setup* s, uint32_t g, const uint8_t* alive, std::vector<uint32_t>* conn) {
-  conn->clear();
-  const uint32_t n0 = s->node_off[g];
-  for (uint32_t i = n0; i < s->node_off[g + 1]; ++i)
+  const uint32_t n0 = s->node_off[g], n1 = s->node_off[g + 1];
+  conn->resize(2 * (s->bond_offset[n1] - s->bond_offset[n0]));  // at most one pair per row entry
+  uint32_t* o = conn->data();
+  size_t k = 0;
+  for (uint32_t i = n0; i < n1; ++i)
     for (uint64_t b = s->bond_offset[i]; b < s->bond_offset[i + 1]; ++b) {
       if (alive && !alive[b]) continue;
-      uint32_t q = s->bond_local[b];
+      const uint32_t q = s->bond_local[b];
       if (i - n0 < q) {
-        conn->push_back(i - n0);
-        conn->push_back(q);
+        o[k++] = i - n0;
+        o[k++] = q;
       }
     }
+  conn->resize(k);
 }
 
 extern "C" int pg_setup_save(pg_setup* s, const char* path) {
