@@ -218,6 +218,12 @@ int pg_get_pair_log(pg_handle* h, uint32_t n, uint64_t* count, uint64_t* hash);
 /* Sticky device error word (PG_ECAPACITY/PG_ERANGE/...), 0 if none; also "nodes too close"
  * events (dir_norm == 0 in contact.h:737) counted since creation. */
 int pg_get_device_status(pg_handle* h, int32_t* status, uint64_t* too_close_events);
+/* Test hook for the failure path of the bounded device waits: presets the arrival count of the
+ * cooperative grid build's barrier, so that its next wait cannot complete; the blocks give up
+ * after the poll limit (~0.3 s) and the step's status becomes PG_ETIMEOUT. The handle keeps that
+ * sticky status (create a new one afterwards). PG_EINVAL without candidate lists or cooperative
+ * launch. */
+int pg_debug_grid_barrier(pg_handle* h, uint32_t arrivals);
 /* Launch configuration in use (after autotuning): force-kernel block size, grid cells per node. */
 int pg_get_launch_config(pg_handle* h, uint32_t* block_size, uint32_t* cells_per_node);
 /* Contact candidate-list skin in use (fraction of R_c; 0: grid search every step). */

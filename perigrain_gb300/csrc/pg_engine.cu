@@ -1145,6 +1145,14 @@ int pg_get_pair_log(pg_handle* h, uint32_t n, uint64_t* count, uint64_t* hash) {
   return PG_OK;
 }
 
+int pg_debug_grid_barrier(pg_handle* h, uint32_t arrivals) {
+  if (!h) return fail(PG_EINVAL, "null handle");
+  if (!h->P.gbar || !h->P.coop_blocks) return fail(PG_EINVAL, "no cooperative grid build on this handle");
+  CU(cudaStreamSynchronize(h->stream));
+  CU(cudaMemcpy(h->P.gbar, &arrivals, 4, cudaMemcpyHostToDevice));
+  return PG_OK;
+}
+
 int pg_get_device_status(pg_handle* h, int32_t* status, uint64_t* too_close) {
   if (!h) return fail(PG_EINVAL, "null handle");
   CU(cudaStreamSynchronize(h->stream));

@@ -1,0 +1,37 @@
+"""Failure detection without a GPU fault: the cooperative grid build's barrier waits are bounded;
+a barrier that cannot complete (its arrival count preset from the host) ends the step with
+PG_ETIMEOUT in the status word, the kernel returns and the context stays usable."""
+import time
+
+import pytest
+
+from perigrain_gb300 import Simulation, setups
+from perigrain_gb300 import _native as N
+
+pytestmark = pytest.mark.gpu
+
+
+def test_grid_barrier_wait_times_out_into_status():
+    s = setups.small_pair(dim=2, seed=71)
+    sim = Simulation(s, dt=2e-8, enable_fracture=1, precision="mixed", contact_skin=0.25)
+    N.check(N.lib().pg_debug_grid_barrier(sim.h, 1 << 30))
+    t0 = time.perf_counter()
+    sim.step(1)  # the first step rebuilds the lists: its first grid barrier cannot complete
+    with pytest.raises(N.PerigrainError) as e:
+        sim.synchronize()
+    assert e.value.code == N.PG_ETIMEOUT
+    assert time.perf_counter() - t0 < 60.0
+    sim.close()
+    # the context is intact: a new handle runs and agrees with the one-shot reference state
+    a = Simulation(s, dt=2e-8, enable_fracture=1, precision="mixed", contact_skin=0.25)
+    a.step(20)
+    a.synchronize()
+    assert a.device_status()[0] == 0
+    a.close()
+
+
+def test_debug_hook_needs_the_cooperative_build():
+    s = setups.small_pair(dim=2, seed=72)
+    sim = Simulation(s, dt=2e-8, precision="mixed", contact_skin=0.0)
+    assert N.lib().pg_debug_grid_barrier(sim.h, 1) == N.PG_EINVAL
+    sim.close()
