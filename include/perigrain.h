@@ -220,9 +220,11 @@ int pg_get_pair_log(pg_handle* h, uint32_t n, uint64_t* count, uint64_t* hash);
 int pg_get_device_status(pg_handle* h, int32_t* status, uint64_t* too_close_events);
 /* Test hook for the failure path of the bounded device waits: presets the arrival count of the
  * cooperative grid build's barrier, so that its next wait cannot complete; the blocks give up
- * after the poll limit (~0.3 s) and the step's status becomes PG_ETIMEOUT. The handle keeps that
- * sticky status (create a new one afterwards). PG_EINVAL without candidate lists or cooperative
- * launch. */
+ * after the poll limit (~0.3 s) and the step's status becomes PG_ETIMEOUT. A handle that timed
+ * out is halted: grid builds already enqueued return at entry (the barrier's arrival count is
+ * stale), and once a status check (pg_synchronize, pg_step_timed, pg_wait, pg_get_device_status)
+ * has reported PG_ETIMEOUT, pg_step returns PG_ETIMEOUT without launching (create a new handle).
+ * PG_EINVAL without candidate lists or cooperative launch. */
 int pg_debug_grid_barrier(pg_handle* h, uint32_t arrivals);
 /* Launch configuration in use (after autotuning): force-kernel block size, grid cells per node. */
 int pg_get_launch_config(pg_handle* h, uint32_t* block_size, uint32_t* cells_per_node);
@@ -317,14 +319,16 @@ int pg_build_bonds(const double* pos, uint32_t n, uint32_t dim, double delta, ui
 const char* pg_bond_last_error(void);
 
 /* pg_build_bonds without any device allocation, for callers that cannot allocate device memory:
- * code running during CUDA-graph capture on its stream, allocator or memory-pool hooks that must
- * not re-enter the allocator, hosts that reserve all device memory up front. This entry point has
- * no counterpart in the reference. Same arguments and results as pg_build_bonds; its scratch is a
- * file-scope device array sized for one grain of at most PG_NOALLOC_MAX_NODES nodes (about 1.7 MB,
- * held by every GPU that loads the library until exit); larger n returns PG_EINVAL. Calls share
- * that array, so calls that overlap on the GPU race; each call clears what it needs. The first
- * call on a device looks the array's address up (make it before any stream capture).
- * pg_noalloc_last_error() describes a failure. */
+ * allocator or memory-pool hooks (a cudaMalloc there would re-enter the allocator they implement)
+ * and hosts that reserve all device memory up front or run under a hard device-memory quota. This
+ * entry point has no counterpart in the reference. Same arguments and results as pg_build_bonds;
+ * its scratch is a file-scope device array sized for one grain of at most PG_NOALLOC_MAX_NODES
+ * nodes (about 1.7 MB, held by every GPU that loads the library until exit); larger n returns
+ * PG_EINVAL. Calls share that array, so calls that overlap on the GPU race; each call clears what
+ * it needs. The first call on a device looks the array's device address up and caches it for the
+ * CUDA context (make that first call before any stream capture; do not call it again on a device
+ * after cudaDeviceReset). It returns after `stream` completes. pg_noalloc_last_error() describes
+ * a failure. */
 #define PG_NOALLOC_MAX_NODES 32768u
 int pg_build_bonds_noalloc(const double* pos, uint32_t n, uint32_t dim, double delta, uint32_t* pairs,
                            uint64_t capacity, uint64_t* n_pairs, void* stream);

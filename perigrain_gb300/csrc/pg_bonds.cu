@@ -22,6 +22,7 @@ namespace pg {
 constexpr int BT = 256;               // threads per block
 constexpr int SCAN_T = 1024;          // scan block
 constexpr int SCAN_TILE_B = SCAN_T * 4;
+static_assert(SCAN_TILE_B == (int)BOND_SCAN_TILE, "scan tile of the bond builder and its declared size differ");
 constexpr int MAX_PARTNERS = 4096;    // partners j > i of one node (the row is sorted in place)
 
 struct BondGrid {
@@ -228,8 +229,8 @@ cudaError_t scan_u32_dev(const uint32_t* in, uint32_t len, uint32_t* out, uint32
   return cudaGetLastError();
 }
 
-uint32_t bond_grid_cells(uint32_t n) { return 4u * n + 64u; }
-uint32_t bond_scan_tiles(uint32_t len) { return cdivb(len ? len : 1, SCAN_TILE_B); }
+uint32_t bond_grid_cells(uint32_t n) { return bond_grid_cells_c(n); }
+uint32_t bond_scan_tiles(uint32_t len) { return bond_scan_tiles_c(len); }
 
 int run_bond_build(const double* pos, uint32_t n, uint32_t dim, double delta, uint32_t* pairs, uint64_t capacity,
                    uint64_t* n_pairs, cudaStream_t st, const BondScratch& S, std::string* err) {

@@ -23,6 +23,13 @@ struct BondScratch {
   uint32_t cells;
 };
 
+// Entries per tile of the bond builder's exclusive scan (1024 threads x 4 entries).
+constexpr uint32_t BOND_SCAN_TILE = 4096;
+// Grid cells of a bond build over n nodes, and scan tiles of a scan over len entries (both also
+// usable where a scratch size must be known at compile time).
+constexpr uint32_t bond_grid_cells_c(uint32_t n) { return 4u * n + 64u; }
+constexpr uint32_t bond_scan_tiles_c(uint32_t len) { return ((len ? len : 1u) + BOND_SCAN_TILE - 1u) / BOND_SCAN_TILE; }
+
 uint32_t bond_grid_cells(uint32_t n);
 // Exclusive scan of in[0..len) into out[0..len], out[len] = total, on stream st. tile_sum holds
 // bond_scan_tiles(len) words; *done must be 0 (and is 0 again when the scan ends).

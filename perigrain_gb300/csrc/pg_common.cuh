@@ -685,6 +685,10 @@ __device__ __forceinline__ bool grid_barrier(const Dev& P, uint32_t* ok_smem) {
         if (++it > GBAR_SPIN_LIMIT) {
           ok = 0;
           set_status(P.status, PG_ETIMEOUT);
+          // the arrival count now holds this launch's stale arrivals: later launches of this
+          // kernel must not use the barrier (an early release would let the scan read counts
+          // before every key is in and the scatter write outside the sorted list)
+          atomicExch(P.gbar + 2, 1u);
           break;
         }
         __nanosleep(64);
@@ -704,6 +708,9 @@ static __global__ void __launch_bounds__(SCAN_THREADS) k_grid_coop(const Dev P) 
   __shared__ uint32_t ok;
   __shared__ bool last;
   if (!*P.rebuild) return;  // set by the predict kernel before this launch: the same for every block
+  // a barrier of an earlier launch timed out: the handle is halted (the host refuses further steps
+  // once it sees PG_ETIMEOUT; launches already enqueued return here)
+  if (((volatile uint32_t*)P.gbar)[2]) return;
   const uint32_t nthr = gridDim.x * blockDim.x;
   // 1. grid keys and per-cell ranks
   for (uint32_t d = blockIdx.x * blockDim.x + threadIdx.x; d < P.N; d += nthr) {

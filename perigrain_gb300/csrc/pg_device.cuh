@@ -161,7 +161,8 @@ struct Dev {
   unsigned long long* sorted_key;
   uint32_t *scan_tile_sum;
   uint32_t *scan_done;
-  uint32_t* gbar;      // [2] grid barrier of the cooperative grid build: arrivals, generation
+  uint32_t* gbar;      // [3] grid barrier of the cooperative grid build: arrivals, generation,
+                       // halted (set when a wait timed out; the build then returns at entry)
   uint32_t coop_blocks;  // blocks of that launch (all resident), 0 = separate grid kernels
   // bonds (SELL-32)
   uint32_t *chunk_slot, *chunk_deg, *chunk_word, *node_deg;

@@ -798,8 +798,8 @@ static int create_impl(const pg_setup_desc* s, const pg_config* cfg_in, pg_handl
     CU(h->dalloc(&P.sorted_key, N));
     for (int p = 0; p < 2; ++p) CU(h->dalloc(&h->rebuild_pp[p], 1));
     P.rebuild = h->rebuild_pp[0];
-    CU(h->dalloc(&P.gbar, 2));
-    CU(cudaMemset(P.gbar, 0, 8));
+    CU(h->dalloc(&P.gbar, 3));
+    CU(cudaMemset(P.gbar, 0, 12));
     P.coop_blocks = grid_coop_blocks(P, h->device);
     CU(cudaMemset(P.cand_n, 0, N));
     CU(cudaMemset(P.disp_b, 0, (size_t)N * SF * 4));
@@ -842,6 +842,7 @@ int check_device_status(pg_handle* h) {
   int32_t st = 0;
   CU(cudaMemcpyAsync(&st, h->P.status, 4, cudaMemcpyDeviceToHost, h->stream));
   CU(cudaStreamSynchronize(h->stream));
+  if (st == PG_ETIMEOUT) h->halted = true;
   return device_status_fail(st);
 }
 
@@ -849,6 +850,8 @@ extern "C" {
 
 int pg_step(pg_handle* h, uint32_t nsteps) {
   if (!h) return fail(PG_EINVAL, "null handle");
+  // after a bounded device wait ran out, the grid build's barrier state is stale: no more steps
+  if (h->halted) return fail(PG_ETIMEOUT, "handle halted: a device wait timed out in an earlier step");
   uint64_t launches = 0;
   if (h->timing) {
     // timed mode: plain launches with CUDA events around every force kernel
@@ -1160,6 +1163,7 @@ int pg_get_device_status(pg_handle* h, int32_t* status, uint64_t* too_close) {
   unsigned long long tc = 0;
   CU(cudaMemcpy(&st, h->P.status, 4, cudaMemcpyDeviceToHost));
   CU(cudaMemcpy(&tc, h->P.too_close, 8, cudaMemcpyDeviceToHost));
+  if (st == PG_ETIMEOUT) h->halted = true;
   if (status) *status = st;
   if (too_close) *too_close = tc;
   return PG_OK;

@@ -169,6 +169,8 @@ struct pg_handle {
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   bool overlap = false;
   bool xpos_separate = false;
+  // set when a status check saw PG_ETIMEOUT (a bounded device wait ran out): pg_step refuses
+  bool halted = false;
   std::vector<void*> allocs;
   // host copies needed for mapping
   std::vector<uint64_t> bond_offset;  // reference CSR

@@ -113,6 +113,7 @@ int pg_wait(pg_handle* h) {
   std::memcpy(&tc, sm + o_st + 8, 8);
   if (s->d.too_close_events) *s->d.too_close_events = tc;
   if (s->d.last_step) *s->d.last_step = s->last_step;
+  if (st == PG_ETIMEOUT) h->halted = true;
   return device_status_fail((int32_t)st);
 }
 

@@ -5,7 +5,8 @@ config/main.conf, runs the reference (debdeepbh/perigrain's own src/ headers and
 compiled unmodified against the project's Eigen/HDF5 API shims by oracle/Makefile) and stores
 every tc_%05u.h5 / wall_%05u.h5 it writes into tests/golden/<case>.npz.
 
-Needs the reference checkout (REF, default /root/reference). Run from the repository root:
+Needs the reference build of oracle/Makefile (the reference checkout is named by PERIGRAIN_REFERENCE
+or the recipe's default). Run from the repository root:
     python tests/golden/make_golden.py
 """
 import hashlib

@@ -1,7 +1,8 @@
 """Golden vectors of the incircle packing, produced by the reference's own code.
 
-Runs get_incenter_mesh_loc from the reference's exp_dict.py (it must be importable from
-/root/reference; this script runs in the development container only, its outputs are committed).
+Runs get_incenter_mesh_loc from the reference's exp_dict.py, imported from the reference checkout
+(PERIGRAIN_REFERENCE, else the development container's checkout; this script runs there only, its
+outputs are committed).
 The reference's third-party imports that are absent here are replaced by stand-ins:
   genmesh   returns the test mesh (PackMesh from perigrain_gb300.packing: seeded structured
             meshes of a rectangle / cube) in the layout genmesh.py:160-291 returns
@@ -21,7 +22,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
-REF = "/root/reference"
+REF = os.environ.get("PERIGRAIN_REFERENCE") or "/root/reference"
 sys.path.insert(0, ROOT)
 
 from perigrain_gb300.packing import cube_mesh, rect_mesh  # noqa: E402

@@ -10,9 +10,11 @@ import pytest
 import _oracle as O
 from perigrain_gb300 import setups
 
-REF = os.environ.get("PERIGRAIN_REFERENCE", "/root/reference")
-pytestmark = pytest.mark.skipif(not os.path.exists(os.path.join(REF, "src", "particle", "timeloop.h")),
-                                reason="reference checkout not present")
+# the reference simulator built from its own sources by oracle/Makefile (absent where the reference
+# checkout is absent)
+O.build_oracle()
+pytestmark = pytest.mark.skipif(not all(os.path.exists(O.REF_BIN[k]) for k in (2, 3)),
+                                reason="reference build (oracle/_ref) not present")
 
 
 def _compare(s, conf):

@@ -1,5 +1,6 @@
 """pg_build_bonds_noalloc, the bond-list builder for callers that cannot allocate device memory
-(graph-capture code, allocator hooks, fixed-budget hosts): called through the C ABI, it must give
+(allocator hooks that must not re-enter the allocator, hosts with a fixed device-memory budget):
+called through the C ABI, it must give
 exactly the pairs of the allocating pg_build_bonds, on two calls in a row (the shared scratch keeps
 the first call's contents, so the second call proves it clears what it needs). Kept in its own
 file, collected last."""
