@@ -13,8 +13,9 @@ than L2), with block size and grid density picked by the project autotuner, over
 whole configured run by default (10,000 steps for the ensemble: the cost of a step grows as the
 collisions bring grains into contact). Beside it: the plain
 FP64 path on the same batch (`plain_fp64`), 256 sequential single-instance FP64 runs
-(`sequential_fp64`, timed on a sample of instances), the mixed-vs-FP64 position error after the
-same steps and the FP64 perturbation floor of these chaotic dynamics (`accuracy`). `e2e` goes
+(`sequential_fp64`, timed on a sample of instances), and mixed-vs-FP64 errors of positions,
+velocities and wall reactions over the whole configured run of every workload beside the spread of
+FP64 runs perturbed at FP32 resolution (`accuracy`; the dynamics are chaotic). `e2e` goes
 through the C ABI from host buffers: setup upload + the timed steps + a tc_-snapshot download
 (CurrPos, vel, acc, force) every 100 steps.
 """
@@ -33,7 +34,6 @@ sys.path.insert(0, ROOT)
 
 METRIC = "node-steps/s"
 COMPARE_STEPS = 1000  # the FP64 path is timed over the first steps only (it is ~20x slower)
-ACCURACY_STEPS = 405  # horizon of the mixed-vs-FP64 position error (chaotic dynamics)
 # Algorithmic bytes of the dominant kernel (the fused bond + contact + wall + integrate kernel),
 # counting each array once per launch and treating neighbour gathers as cache-served:
 #   FP64:  per node  reads disp, xpos, cur, vel, acc, extforce (8*dim B each), vol (8), grain id
@@ -198,16 +198,31 @@ def instance_subset(setup, first, count):
     return sub
 
 
-def cpu_reference(setup, spec, steps, threads, budget_s=12.0):
-    """The reference's CPU algorithm, timed on a bounded sample of the workload: the oracle port
-    in reference-structured mode (the reference's node-pair loops, bit-identical arithmetic),
-    independent instances run concurrently on `threads` host threads, for up to `steps` steps or
-    until `budget_s` seconds of work have been done."""
+def cpu_model():
+    """The host CPU's model name (lscpu on Arm, /proc/cpuinfo on x86), or the machine type."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith("model name"):
+                    return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+
+    return platform.machine()
+
+
+def _cpu_rate(sub, spec, steps, threads, budget_s):
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import _oracle as O
 
-    take = min(setup.n_instances, max(1, threads))
-    sub = instance_subset(setup, 0, take)
     sim = O.OracleSim(sub, dt=spec["dt"], enable_fracture=1)
     sim.set_mode(1, threads)
     t0 = time.perf_counter()
@@ -218,8 +233,30 @@ def cpu_reference(setup, spec, steps, threads, budget_s=12.0):
         if time.perf_counter() - t0 > budget_s:
             break
     dt = time.perf_counter() - t0
-    return sub.n_nodes * done / dt, dict(kind="port", cores=threads, steps=done, instances=take,
-                                         nodes=sub.n_nodes, seconds=round(dt, 3))
+    return sub.n_nodes * done / dt, done, dt
+
+
+def cpu_reference(setup, spec, steps, threads, budget_s=12.0, one_thread_s=4.0):
+    """The reference's CPU algorithm, timed on a bounded sample of the workload: the oracle port
+    in reference-structured mode (the reference's node-pair loops, bit-identical arithmetic),
+    independent instances run concurrently on `threads` host threads (one instance per thread, the
+    reference's OpenMP loop over grains gives no more parallelism than that for two-grain
+    instances), for up to `steps` steps or until `budget_s` seconds of work have been done. The
+    instances are independent, so the rate of the sample is the rate of the whole ensemble on these
+    cores (work grows linearly with the number of instances). Beside it: one instance on one thread
+    for up to `one_thread_s` seconds."""
+    take = min(setup.n_instances, max(1, threads))
+    sub = instance_subset(setup, 0, take)
+    v, done, dt = _cpu_rate(sub, spec, steps, threads, budget_s)
+    one = instance_subset(setup, 0, 1)
+    v1, done1, dt1 = _cpu_rate(one, spec, steps, 1, one_thread_s)
+    return v, dict(kind="port", cores=threads, steps=done, instances=take, nodes=sub.n_nodes, seconds=round(dt, 3),
+                   cpu_model=cpu_model(), nproc=os.cpu_count(),
+                   one_thread={"value": v1, "unit": METRIC, "instances": 1, "nodes": one.n_nodes, "steps": done1,
+                               "seconds": round(dt1, 3)},
+                   scaling="%d of %d independent instances, one per thread; the ensemble's CPU time grows "
+                           "linearly with its instances, so this rate is the whole ensemble's rate on %d threads"
+                           % (take, setup.n_instances, threads))
 
 
 def adjoint_bench(n_steps=5000, checkpoint_every=100, n_fd=4):
@@ -479,6 +516,164 @@ def packing_bench(nx=800, ny=500, repeats=3):
                                        % (len(crad), cpu_s)}}
 
 
+ACC_HORIZONS = (10, 100, 1000, 10000)  # pointwise comparisons (and the configured run's last step)
+ACC_WINDOWS = 10  # wall-reaction time series compared as means over this many windows of the run
+ACC_EPS = 2.0 ** -24  # FP32 unit round-off: size of the FP64 ensemble's velocity perturbation
+ACC_POS_TOL = 1e-6  # pointwise relative position error bound while the dynamics do not amplify
+# whole-run statistics: a mixed-vs-FP64 difference passes when it is at most max(2 x the FP64
+# ensemble's spread, floor); the floors are relative to the statistic's FP64 scale
+ACC_STAT_FLOOR = {"kinetic_energy": 2e-2, "mean_grain_speed": 5e-2, "grain_centroid": 2e-2,
+                  "reaction_window_means": 5e-2, "broken_bonds": 1e-1}
+
+
+def _rel(a, b):
+    """max |a - b| / max |b| over all entries (0 when both vanish)."""
+    s = float(np.abs(b).max()) if np.size(b) else 0.0
+    d = float(np.abs(a - b).max()) if np.size(b) else 0.0
+    return d / s if s > 0 else (0.0 if d == 0 else float("inf"))
+
+
+def perturbed_velocities(setup, seed, eps=ACC_EPS):
+    """Copy of a setup whose initial velocity components are moved by eps * V with seeded random
+    signs, V = max(max |v0|, 1 m/s): FP64 inputs known only to FP32 resolution."""
+    p = setup.copy()
+    rng = np.random.default_rng(1000 + seed)
+    V = max(float(np.abs(setup.vel).max()), 1.0)
+    p.vel = setup.vel + eps * V * rng.choice([-1.0, 1.0], size=setup.vel.shape)
+    return p
+
+
+def accuracy_config(k, members=2, sample_every=100, horizons=ACC_HORIZONS):
+    """Mixed precision against FP64 over the whole configured run of workload k.
+
+    Runs of the same setup advance together: the mixed path, the FP64 path (the reference's
+    arithmetic, bit-exact to it in the tests) and an ensemble of `members` FP64 runs whose initial
+    velocities differ from the setup's at FP32 resolution (perturbed_velocities). Contact dynamics
+    are chaotic -- an FP64 run perturbed by 1e-15 already moves by several percent after a
+    collision -- so every mixed-vs-FP64 figure is reported beside the ensemble's spread, the largest
+    difference of an ensemble run from the FP64 run in the same measure.
+
+      pointwise  at each horizon: max|dx| / max|x| (CurrPos), max|dv| / max|v| (vel) and
+                 max|dR| / max|R| (wall reactions, every instance and side)
+      full_run   kinetic energy sum(1/2 rho vol |v|^2) sampled every `sample_every` steps (max
+                 difference / max KE), the wall-reaction time series (sampled like the reference's
+                 wall_ files every `sample_every` steps) as means over ACC_WINDOWS windows, the mean
+                 grain speed and the grain centroids (mass-weighted) at the end, the number of bonds
+                 broken (relative to FP64's), and the drift of total linear momentum (configurations
+                 without walls, where the reference conserves it) relative to sum(m |v0|).
+    A whole-run measure passes when the mixed difference is at most max(2 x spread,
+    ACC_STAT_FLOOR[measure]); pointwise, the horizon through which the position error stays within
+    ACC_POS_TOL is reported.
+    """
+    from perigrain_gb300 import Simulation, setups
+
+    spec = setups.WORKLOADS[k]
+    setup = setups.workload(k)
+    steps = spec["steps"]
+    t0 = time.perf_counter()
+    sims = {"mixed": Simulation(setup, **engine_kwargs(spec, "mixed")),
+            "fp64": Simulation(setup, **engine_kwargs(spec, "fp64"))}
+    ens = ["ens%d" % i for i in range(members)]
+    for i, name in enumerate(ens):
+        sims[name] = Simulation(perturbed_velocities(setup, i), **engine_kwargs(spec, "fp64"))
+    D = setup.dim
+    gsize = np.diff(setup.grain_node_offset.astype(np.int64))
+    m = (setup.vol * np.repeat(setup.rho, gsize))[:, None]
+    starts = setup.grain_node_offset[:-1].astype(np.int64)
+    gmass = np.add.reduceat(m[:, 0], starts)
+    v0 = setup.vel.reshape(-1, D)
+    p0 = (m * v0).sum(0)
+    pscale = max(float((m * np.abs(v0)).sum()), 1e-300)
+    walls = bool(np.any(setup.allow_wall))
+    hz = sorted(set([h for h in horizons if h < steps] + [steps]))
+    ke = {n: [] for n in sims}
+    reac = {n: [] for n in sims}
+    mom = {n: 0.0 for n in sims}
+    point = []
+    done = 0
+    while done < steps:
+        nxt = min([h for h in hz if h > done] + [done + sample_every, steps])
+        for sm in sims.values():
+            sm.step(nxt - done)
+        done = nxt
+        vel = {}
+        for name, sm in sims.items():
+            v = sm.field("vel")
+            ke[name].append(0.5 * float((m[:, 0] * (v * v).sum(1)).sum()))
+            if walls:
+                reac[name].append(sm.reaction())
+            else:
+                mom[name] = max(mom[name], float(np.abs((m * v).sum(0) - p0).max()) / pscale)
+            vel[name] = v
+        if done in hz:
+            x = {name: sm.field("CurrPos") for name, sm in sims.items()}
+            row = {"step": done}
+            for key, group in (("mixed", ["mixed"]), ("spread", ens)):
+                row[key] = {"pos": max(_rel(x[g], x["fp64"]) for g in group),
+                            "vel": max(_rel(vel[g], vel["fp64"]) for g in group)}
+                if walls:
+                    row[key]["reaction"] = max(_rel(reac[g][-1], reac["fp64"][-1]) for g in group)
+            row["pos_within_tol"] = row["mixed"]["pos"] <= ACC_POS_TOL
+            point.append(row)
+    fin = {}
+    for name, sm in sims.items():
+        x, v = sm.field("CurrPos"), sm.field("vel")
+        alive = sm.bond_alive()
+        gv = np.add.reduceat(m * v, starts, axis=0) / gmass[:, None]
+        fin[name] = {"gspeed": float(np.sqrt((gv * gv).sum(1)).mean()),
+                     "gpos": np.add.reduceat(m * x, starts, axis=0) / gmass[:, None],
+                     "broken": int(setup.n_bonds - int(alive.sum()))}
+        sm.close()
+    kef = {n: np.array(v) for n, v in ke.items()}
+    kscale = float(kef["fp64"].max())
+    w = None
+    if walls:
+        nwin = min(ACC_WINDOWS, len(reac["fp64"]))
+        w = np.array_split(np.arange(len(reac["fp64"])), nwin)
+    bscale = max(fin["fp64"]["broken"], 1)
+    sscale = max(fin["fp64"]["gspeed"], 1e-300)
+
+    def measure(g):
+        e = {"kinetic_energy": float(np.abs(kef[g] - kef["fp64"]).max() / kscale) if kscale > 0 else 0.0,
+             "mean_grain_speed": abs(fin[g]["gspeed"] - fin["fp64"]["gspeed"]) / sscale,
+             "grain_centroid": _rel(fin[g]["gpos"], fin["fp64"]["gpos"]),
+             "broken_bonds": abs(fin[g]["broken"] - fin["fp64"]["broken"]) / bscale}
+        if walls:
+            a, b = np.array(reac[g]), np.array(reac["fp64"])
+            e["reaction_window_means"] = _rel(np.stack([a[i].mean(0) for i in w]), np.stack([b[i].mean(0) for i in w]))
+        return e
+
+    mixed = measure("mixed")
+    spread = {key: max(measure(g)[key] for g in ens) for key in mixed} if ens else {key: 0.0 for key in mixed}
+    full = {key: {"mixed": mixed[key], "spread": spread[key], "floor": ACC_STAT_FLOOR[key],
+                  "pass": mixed[key] <= max(2.0 * spread[key], ACC_STAT_FLOOR[key])} for key in mixed}
+    full["broken_bond_counts"] = {n: fin[n]["broken"] for n in ("mixed", "fp64")}
+    full["mean_grain_speed_values"] = {n: fin[n]["gspeed"] for n in ("mixed", "fp64")}
+    if not walls:
+        full["momentum_drift"] = {"mixed": mom["mixed"], "fp64": mom["fp64"], "pass": mom["mixed"] <= 1e-6}
+    tol_h = [r["step"] for r in point if r["pos_within_tol"]]
+    return {"workload": spec["name"], "dim": D, "nodes": setup.n_nodes, "bonds": setup.n_bonds, "steps": steps,
+            "dt": spec["dt"], "ensemble": members, "pos_err_le_1e-6_through_step": max(tol_h) if tol_h else 0,
+            "pointwise": point, "full_run": full,
+            "all_full_run_pass": all(v["pass"] for v in full.values() if isinstance(v, dict) and "pass" in v),
+            "seconds": time.perf_counter() - t0}
+
+
+def accuracy_report(configs=(0, 1, 2, 3, 4), members=2):
+    return {"runs": [accuracy_config(k, members=members) for k in configs],
+            "measures": "'mixed': mixed vs FP64; 'spread': the largest difference from FP64 of %d FP64 runs whose "
+                        "initial velocities are perturbed by 2^-24 max(|v0|, 1 m/s) with random signs" % members,
+            "tolerance": ACCURACY_TOLERANCE}
+
+
+ACCURACY_TOLERANCE = (
+    "pointwise: relative position error <= 1e-6 up to the step given per workload (the dynamics then amplify "
+    "any difference; later horizons are reported beside the FP64 ensemble spread); whole run: each statistic "
+    "differs from FP64 by at most max(2 x ensemble spread, floor) -- kinetic-energy series and grain centroids "
+    "2e-2, mean grain speed and windowed wall-reaction means 5e-2, broken-bond count 1e-1 (relative); momentum "
+    "drift <= 1e-6 of sum(m|v0|) without walls")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -498,6 +693,12 @@ def main():
                          "(checkpoint every 100; the command profiled under ncu)")
     ap.add_argument("--profile-packing", type=int, default=0, metavar="NX",
                     help="only incircle packings of an NX x 0.625 NX-cell mesh (the command profiled under ncu)")
+    ap.add_argument("--accuracy", default="full", choices=["full", "off"],
+                    help="mixed-vs-FP64 error over the whole configured run of every workload (default full)")
+    ap.add_argument("--accuracy-members", type=int, default=2,
+                    help="FP64 runs perturbed at FP32 resolution per workload in the accuracy report")
+    ap.add_argument("--accuracy-only", default="", metavar="K,K,...",
+                    help="only the accuracy report of these workloads (e.g. 0,1,2,3,4); prints one JSON line")
     ap.add_argument("--profile-run", action="store_true",
                     help="only warmup + steps of the engine (the command profiled under ncu)")
     a = ap.parse_args()
@@ -521,13 +722,21 @@ def main():
                            "nodes_sampled": info["nodes"]},
                 "cpu_baseline": dict(value=v, unit=METRIC, kind=info["kind"], cores=info["cores"],
                                      sample="%d instances x %d steps of %s, reference-structured oracle port"
-                                            % (info["instances"], info["steps"], spec["name"])),
+                                            % (info["instances"], info["steps"], spec["name"]),
+                                     cpu_model=info["cpu_model"], nproc=info["nproc"], one_thread=info["one_thread"],
+                                     scaling=info["scaling"]),
                 "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
         return
 
     import perigrain_gb300 as pg
     from perigrain_gb300 import Simulation
+
+    if a.accuracy_only:
+        pg.engine.select_device(local_rank)
+        print(json.dumps(accuracy_report([int(x) for x in a.accuracy_only.split(",")], members=a.accuracy_members)),
+              flush=True)
+        return
 
     if a.profile_packing:
         import torch
@@ -623,30 +832,19 @@ def main():
         s64.step(min(k_cmp, 200))
         f64_ms, t64_ms, n64 = s64.kernel_times()
         s64.close()
+        f64_launch_s = f64_ms / max(1, n64) / 1e3
+        peak64, peak64_kind = load_peaks()
+        hbm64 = node_step_bytes(setup.n_nodes, setup.n_bonds, setup.dim, "fp64") / f64_launch_s / 1e9
+        tf64 = setup.n_bonds * fp64_flops_per_bond(setup.dim) / f64_launch_s / 1e12
         plain = {"value": setup.n_nodes * k_cmp / (ms64 / 1e3), "unit": METRIC, "ms_per_step": ms64 / k_cmp,
                  "steps": k_cmp, "mixed_same_steps": setup.n_nodes * k_cmp / (ms_cmp / 1e3),
                  "k_force_ms": f64_ms / max(1, n64),
-                 "fp64_tflops": setup.n_bonds * fp64_flops_per_bond(setup.dim) / (f64_ms / max(1, n64) / 1e3) / 1e12}
-        # accuracy over ACCURACY_STEPS steps: mixed vs FP64, and the chaos floor (FP64 again with one
-        # velocity component changed by one ulp)
-        total_steps = ACCURACY_STEPS
-        runs = []
-        for prec, stp in (("mixed", setup), ("fp64", setup), ("fp64", None)):
-            if stp is None:
-                stp = setup.copy()
-                k = int(setup.grain_node_offset[1]) * setup.dim
-                stp.vel[k] = np.nextafter(stp.vel[k], np.inf)
-            r = Simulation(stp, **engine_kwargs(spec, prec))
-            r.step(total_steps)
-            runs.append(r.field("CurrPos"))
-            r.close()
-        x_main, x64, xf = runs
-        scale = np.abs(x64).max()
-        accuracy = {"steps": total_steps, "pos_rel_err_mixed_vs_fp64": float(np.abs(x_main - x64).max() / scale),
-                    "fp64_one_ulp_perturbation_floor": float(np.abs(xf - x64).max() / scale),
-                    "note": "max|dx| / max|x| over all nodes; the FP64 engine is bit-identical to the "
-                            "reference's arithmetic (tests), the floor is FP64 vs FP64 with one velocity "
-                            "component moved by one ulp"}
+                 "roofline": {"kernel": "k_force", "bound": "fp64 pipe",
+                              "hbm_achieved": hbm64, "hbm_peak": peak64, "hbm_frac": hbm64 / peak64,
+                              "hbm_peak_source": peak64_kind,
+                              "bytes_model": "per node-step B = (8 dim + 1) 8 + 12.125 deg + 16",
+                              "fp64_tflops": tf64, "fp64_nominal_tflops": 1.25, "fp64_frac_of_nominal": tf64 / 1.25},
+                 "fp64_tflops": tf64}
         # 256 sequential single-instance FP64 runs, timed on a sample of instances
         ns = min(8, setup.n_instances)
         k_seq = min(a.steps, 200)
@@ -718,6 +916,10 @@ def main():
     fp64_tflops = setup.n_bonds * fp64_flops_per_bond(D) / (force_launch_ms / 1e3) / 1e12
     traffic = profiled_traffic("%s/%s" % (spec["name"], a.precision))
     cpu_v, cpu_info = cpu_reference(setup, spec, a.cpu_steps, threads)
+    if a.precision == "mixed" and a.accuracy == "full":
+        # mixed vs FP64 over the whole configured run of every workload (one perturbed FP64 run each
+        # bounds the bench's time; --accuracy-only with --accuracy-members 2 gives the wider ensemble)
+        accuracy = accuracy_report(members=1)
     adjoint = None if a.no_adjoint else adjoint_bench()
     packing_line = None if a.no_packing else packing_bench()
     bonds_line = None if a.no_packing else bonds_bench()
@@ -752,7 +954,9 @@ def main():
         "cpu_baseline": {"value": cpu_v, "unit": METRIC, "cores": cpu_info["cores"], "kind": cpu_info["kind"],
                          "sample": "%d instances x %d steps of %s (%d nodes), reference-structured oracle port, "
                                    "%.1f s" % (cpu_info["instances"], cpu_info["steps"], spec["name"],
-                                               cpu_info["nodes"], cpu_info["seconds"])},
+                                               cpu_info["nodes"], cpu_info["seconds"]),
+                         "cpu_model": cpu_info["cpu_model"], "nproc": cpu_info["nproc"],
+                         "one_thread": cpu_info["one_thread"], "scaling": cpu_info["scaling"]},
         "e2e": {"value": e2e_nodes * e2e_steps / (e2e_ms / 1e3), "unit": METRIC, "steps": e2e_steps,
                 "h2d_bytes_per_step": h2d / e2e_steps, "d2h_bytes_per_step": d2h / e2e_steps,
                 "note": "pg_create from host arrays + %d steps + %d tc_ snapshots (one every 100 steps, copied to "
