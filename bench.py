@@ -259,15 +259,18 @@ def cpu_reference(setup, spec, steps, threads, budget_s=12.0, one_thread_s=4.0):
                            % (take, setup.n_instances, threads))
 
 
-def adjoint_bench(n_steps=5000, checkpoint_every=100, n_fd=4):
-    """Cost and checks of the gradient path on the differentiable compaction (50 grains, 5000
-    steps, mixed-precision forward): backward (recompute from checkpoints + reverse steps) time
-    over forward (with checkpointing) time, the FP64 reference gradient (FP64 replay of the same
-    masks) and central differences of the frozen FP64 map for the largest sensitivities."""
-    from perigrain_gb300 import Simulation, grad, setups
+GRAD_HORIZONS = (200, 500, 1000, 2000, 5000)  # steps at which the gradient checks are repeated
+GRAD_TOL = 1e-2  # a check holds at a horizon when its error is within this of the largest sensitivity
 
-    spec = setups.WORKLOADS[4]
-    s = setups.workload(4)
+
+def _grad_checks(s, spec, n_steps, checkpoint_every=100, n_fd=4, times=False):
+    """One differentiable run of n_steps steps of setup s: the mixed-precision gradient of
+    J = top-wall reaction (y) / |value| + kinetic energy / value with respect to the per-grain
+    parameters, the FP64 reference gradient (FP64 replay of the same masks, FP64 reverse step) and
+    central differences of the frozen FP64 map for the n_fd largest sensitivities at h = 1e-4 and
+    1e-6 (relative). Errors are relative to the largest reference sensitivity theta dJ/dtheta."""
+    from perigrain_gb300 import Simulation, grad
+
     sim = Simulation(s, dt=spec["dt"], precision="mixed")
     run = grad.GradRun(sim, n_steps, checkpoint_every)
     r0, ke0 = run.forward()
@@ -275,16 +278,20 @@ def adjoint_bench(n_steps=5000, checkpoint_every=100, n_fd=4):
     wr = np.zeros_like(r0)
     wr[0, 2, 1] = 1.0 / abs(top) if top else 0.0
     wk = 1.0 / ke0
-    run.backward(reaction_bar=wr, ke_bar=wk)  # first call captures the segment graphs
-    run.forward()
+    out = {"steps": n_steps}
+    if times:
+        run.backward(reaction_bar=wr, ke_bar=wk)  # the first call captures the segment graphs
+        run.forward()
     g = run.backward(reaction_bar=wr, ke_bar=wk)
-    t = run.times()
+    if times:
+        out["times"] = run.times()
     th = run.params()
     tv = np.stack([th[k] for k in grad.PARAMS], 1)
     sens = g * tv
     m = run.record_masks()
     run.forward(m)
     g_ref = run.backward(reaction_bar=wr, ke_bar=wk) * tv
+    scale = float(np.abs(g_ref).max())
     idx = np.argsort(-np.abs(g_ref).ravel())[:n_fd]
     fd_err = {}
     for h in (1e-4, 1e-6):
@@ -300,20 +307,49 @@ def adjoint_bench(n_steps=5000, checkpoint_every=100, n_fd=4):
                 vals.append(float((wr * r).sum() + (wk * ke).sum()))
             run.set_params(**{k: th[k] for k in grad.PARAMS})
             e = max(e, abs((vals[0] - vals[1]) / (2 * h) - g_ref[gi, a]))
-        fd_err["h=%g" % h] = e / np.abs(g_ref).max()
+        fd_err["h=%g" % h] = e / scale
     m.close()
     sim.close()
+    out.update({"max_abs_sensitivity": float(np.abs(sens).max()),
+                "mixed_vs_fp64_reference_grad_gap": float(np.abs(sens - g_ref).max() / scale),
+                "fd_vs_fp64_adjoint_top%d" % n_fd: fd_err})
+    return out
+
+
+def adjoint_bench(n_steps=5000, checkpoint_every=100, n_fd=4, horizons=GRAD_HORIZONS):
+    """Cost and checks of the gradient path on the differentiable compaction (50 grains, 5000
+    steps, mixed-precision forward): backward (recompute from checkpoints + reverse steps) time
+    over forward (with checkpointing) time at the configured 5000 steps, and at each horizon the
+    gap between the mixed-precision gradient and the FP64 reference gradient and central
+    differences of the frozen FP64 map for the largest sensitivities. The compaction is chaotic
+    (FP64 runs perturbed at FP32 resolution separate), so the checks hold up to a horizon; the line
+    names the longest horizon at which all of them are within GRAD_TOL."""
+    from perigrain_gb300 import setups
+
+    spec = setups.WORKLOADS[4]
+    s = setups.workload(4)
+    full = _grad_checks(s, spec, n_steps, checkpoint_every, n_fd, times=True)
+    t = full.pop("times")
+    checks = [_grad_checks(s, spec, h, checkpoint_every, n_fd) for h in horizons if h < n_steps] + [full]
+    fdk = "fd_vs_fp64_adjoint_top%d" % n_fd
+    for c in checks:
+        c["hold"] = bool(c["mixed_vs_fp64_reference_grad_gap"] <= GRAD_TOL and c[fdk]["h=1e-06"] <= GRAD_TOL
+                         and c[fdk]["h=0.0001"] <= GRAD_TOL)
+    held = [c["steps"] for c in checks if c["hold"]]
+    through = 0
+    for c in checks:  # the horizon through which every check holds at every shorter horizon too
+        if not c["hold"]:
+            break
+        through = c["steps"]
     return {"workload": spec["name"], "steps": n_steps, "checkpoint_every": checkpoint_every, "nodes": s.n_nodes,
             "params": 4 * s.n_grains, "objective": "top-wall reaction (y) / |value| + kinetic energy / value",
             "forward_ms": t["forward_ms"], "backward_ms": t["backward_ms"],
             "backward_over_forward": t["backward_ms"] / t["forward_ms"],
             "forward_launches": t["forward_launches"], "backward_launches": t["backward_launches"],
-            "max_abs_sensitivity": float(np.abs(sens).max()),
-            "mixed_vs_fp64_reference_grad_gap": float(np.abs(sens - g_ref).max() / np.abs(g_ref).max()),
-            "fd_vs_fp64_adjoint_top%d" % n_fd: fd_err,
-            "note": "gradient checks are exact at short horizons (tests/test_gpu_grad.py); over 5000 steps the "
-                    "stirred compaction's frozen-mask map is chaotic, so the mixed and FP64 trajectories (and "
-                    "their gradients) separate and h=1e-4 differences are nonlinear"}
+            "checks": checks, "checks_hold_through_step": through, "checks_hold_at": held, "tolerance": GRAD_TOL,
+            "note": "each check is relative to the largest FP64 reference sensitivity; beyond the stated horizon the "
+                    "compaction's chaotic dynamics separate the mixed and FP64 trajectories (and their gradients) and "
+                    "push h=1e-4 differences out of the linear regime"}
 
 
 def bonds_bench(n_target=200_000, repeats=5):
@@ -558,9 +594,11 @@ def accuracy_config(k, members=2, sample_every=100, horizons=ACC_HORIZONS):
       full_run   kinetic energy sum(1/2 rho vol |v|^2) sampled every `sample_every` steps (max
                  difference / max KE), the wall-reaction time series (sampled like the reference's
                  wall_ files every `sample_every` steps) as means over ACC_WINDOWS windows, the mean
-                 grain speed and the grain centroids (mass-weighted) at the end, the number of bonds
-                 broken (relative to FP64's), and the drift of total linear momentum (configurations
-                 without walls, where the reference conserves it) relative to sum(m |v0|).
+                 grain speed at the end, the grain centroids (mass-weighted) at the end as the mean
+                 distance from FP64's over the mean distance the grains travelled, the number of
+                 bonds broken (relative to FP64's), and the drift of total linear momentum
+                 (configurations without walls, where the reference conserves it) relative to
+                 sum(m |v0|).
     A whole-run measure passes when the mixed difference is at most max(2 x spread,
     ACC_STAT_FLOOR[measure]); pointwise, the horizon through which the position error stays within
     ACC_POS_TOL is reported.
@@ -613,7 +651,7 @@ def accuracy_config(k, members=2, sample_every=100, horizons=ACC_HORIZONS):
                             "vel": max(_rel(vel[g], vel["fp64"]) for g in group)}
                 if walls:
                     row[key]["reaction"] = max(_rel(reac[g][-1], reac["fp64"][-1]) for g in group)
-            row["pos_within_tol"] = row["mixed"]["pos"] <= ACC_POS_TOL
+            row["pos_within_tol"] = bool(row["mixed"]["pos"] <= ACC_POS_TOL)
             point.append(row)
     fin = {}
     for name, sm in sims.items():
@@ -624,6 +662,9 @@ def accuracy_config(k, members=2, sample_every=100, horizons=ACC_HORIZONS):
                      "gpos": np.add.reduceat(m * x, starts, axis=0) / gmass[:, None],
                      "broken": int(setup.n_bonds - int(alive.sum()))}
         sm.close()
+    x0 = setup.pos.reshape(-1, D) + setup.disp.reshape(-1, D)
+    gpos0 = np.add.reduceat(m * x0, starts, axis=0) / gmass[:, None]
+    travel = max(float(np.sqrt(((fin["fp64"]["gpos"] - gpos0) ** 2).sum(1)).mean()), 1e-300)
     kef = {n: np.array(v) for n, v in ke.items()}
     kscale = float(kef["fp64"].max())
     w = None
@@ -636,7 +677,7 @@ def accuracy_config(k, members=2, sample_every=100, horizons=ACC_HORIZONS):
     def measure(g):
         e = {"kinetic_energy": float(np.abs(kef[g] - kef["fp64"]).max() / kscale) if kscale > 0 else 0.0,
              "mean_grain_speed": abs(fin[g]["gspeed"] - fin["fp64"]["gspeed"]) / sscale,
-             "grain_centroid": _rel(fin[g]["gpos"], fin["fp64"]["gpos"]),
+             "grain_centroid": float(np.sqrt(((fin[g]["gpos"] - fin["fp64"]["gpos"]) ** 2).sum(1)).mean()) / travel,
              "broken_bonds": abs(fin[g]["broken"] - fin["fp64"]["broken"]) / bscale}
         if walls:
             a, b = np.array(reac[g]), np.array(reac["fp64"])
@@ -646,11 +687,11 @@ def accuracy_config(k, members=2, sample_every=100, horizons=ACC_HORIZONS):
     mixed = measure("mixed")
     spread = {key: max(measure(g)[key] for g in ens) for key in mixed} if ens else {key: 0.0 for key in mixed}
     full = {key: {"mixed": mixed[key], "spread": spread[key], "floor": ACC_STAT_FLOOR[key],
-                  "pass": mixed[key] <= max(2.0 * spread[key], ACC_STAT_FLOOR[key])} for key in mixed}
+                  "pass": bool(mixed[key] <= max(2.0 * spread[key], ACC_STAT_FLOOR[key]))} for key in mixed}
     full["broken_bond_counts"] = {n: fin[n]["broken"] for n in ("mixed", "fp64")}
     full["mean_grain_speed_values"] = {n: fin[n]["gspeed"] for n in ("mixed", "fp64")}
     if not walls:
-        full["momentum_drift"] = {"mixed": mom["mixed"], "fp64": mom["fp64"], "pass": mom["mixed"] <= 1e-6}
+        full["momentum_drift"] = {"mixed": mom["mixed"], "fp64": mom["fp64"], "pass": bool(mom["mixed"] <= 1e-6)}
     tol_h = [r["step"] for r in point if r["pos_within_tol"]]
     return {"workload": spec["name"], "dim": D, "nodes": setup.n_nodes, "bonds": setup.n_bonds, "steps": steps,
             "dt": spec["dt"], "ensemble": members, "pos_err_le_1e-6_through_step": max(tol_h) if tol_h else 0,
@@ -660,9 +701,12 @@ def accuracy_config(k, members=2, sample_every=100, horizons=ACC_HORIZONS):
 
 
 def accuracy_report(configs=(0, 1, 2, 3, 4), members=2):
-    return {"runs": [accuracy_config(k, members=members) for k in configs],
-            "measures": "'mixed': mixed vs FP64; 'spread': the largest difference from FP64 of %d FP64 runs whose "
-                        "initial velocities are perturbed by 2^-24 max(|v0|, 1 m/s) with random signs" % members,
+    """members: FP64 ensemble runs per workload, an int or a dict workload -> int."""
+    mem = members if isinstance(members, dict) else {k: members for k in configs}
+    return {"runs": [accuracy_config(k, members=mem[k]) for k in configs],
+            "measures": "'mixed': mixed vs FP64; 'spread': the largest difference from FP64 of the workload's "
+                        "'ensemble' FP64 runs whose initial velocities are perturbed by 2^-24 max(|v0|, 1 m/s) "
+                        "with random signs",
             "tolerance": ACCURACY_TOLERANCE}
 
 
@@ -670,7 +714,8 @@ ACCURACY_TOLERANCE = (
     "pointwise: relative position error <= 1e-6 up to the step given per workload (the dynamics then amplify "
     "any difference; later horizons are reported beside the FP64 ensemble spread); whole run: each statistic "
     "differs from FP64 by at most max(2 x ensemble spread, floor) -- kinetic-energy series and grain centroids "
-    "2e-2, mean grain speed and windowed wall-reaction means 5e-2, broken-bond count 1e-1 (relative); momentum "
+    "(relative to the grains' travel) 2e-2, mean grain speed and windowed wall-reaction means 5e-2, broken-bond "
+    "count 1e-1 (relative); momentum "
     "drift <= 1e-6 of sum(m|v0|) without walls")
 
 
@@ -695,12 +740,17 @@ def main():
                     help="only incircle packings of an NX x 0.625 NX-cell mesh (the command profiled under ncu)")
     ap.add_argument("--accuracy", default="full", choices=["full", "off"],
                     help="mixed-vs-FP64 error over the whole configured run of every workload (default full)")
+    ap.add_argument("--adjoint-only", action="store_true",
+                    help="only the gradient-path measurement and its checks at every horizon; one JSON line")
     ap.add_argument("--accuracy-members", type=int, default=2,
                     help="FP64 runs perturbed at FP32 resolution per workload in the accuracy report")
     ap.add_argument("--accuracy-only", default="", metavar="K,K,...",
                     help="only the accuracy report of these workloads (e.g. 0,1,2,3,4); prints one JSON line")
     ap.add_argument("--profile-run", action="store_true",
                     help="only warmup + steps of the engine (the command profiled under ncu)")
+    ap.add_argument("--profile-extras", action="store_true",
+                    help="with --profile-run: then one asynchronous tc_ snapshot, one on-device post-processing "
+                         "call and one bond-list build of a 20k-node grain (their kernels profiled under ncu)")
     a = ap.parse_args()
     a.warmup = max(3, a.warmup)
     import perigrain_gb300.setups as _setups
@@ -731,6 +781,11 @@ def main():
 
     import perigrain_gb300 as pg
     from perigrain_gb300 import Simulation
+
+    if a.adjoint_only:
+        pg.engine.select_device(local_rank)
+        print(json.dumps(adjoint_bench()), flush=True)
+        return
 
     if a.accuracy_only:
         pg.engine.select_device(local_rank)
@@ -784,6 +839,18 @@ def main():
     if a.profile_run:
         sim.step(a.steps)
         sim.synchronize()
+        if a.profile_extras:
+            import math
+
+            from perigrain_gb300 import bonds, setups as _s
+
+            got = sim.snapshot(("CurrPos", "vel", "acc", "force")).wait()
+            post = sim.postprocess(node_damage=True)
+            h = 1e-5
+            p, _ = _s.grid_nodes("disk", h * math.sqrt(20000 / math.pi), h, 2, 6, 0.1, np.random.default_rng(5), 0.0)
+            pairs = bonds.build_bonds(np.ascontiguousarray(p, np.float64), 3 * h)
+            print("profile extras: snapshot %d nodes, post-processing of %d grains, %d bonds of a %d-node grain"
+                  % (len(got["CurrPos"]), len(post["grain_damage"]), len(pairs), len(p)))
         print("profile run: %s, %d nodes, %d steps" % (spec["name"], setup.n_nodes, a.warmup + a.steps))
         return
 
@@ -917,9 +984,10 @@ def main():
     traffic = profiled_traffic("%s/%s" % (spec["name"], a.precision))
     cpu_v, cpu_info = cpu_reference(setup, spec, a.cpu_steps, threads)
     if a.precision == "mixed" and a.accuracy == "full":
-        # mixed vs FP64 over the whole configured run of every workload (one perturbed FP64 run each
-        # bounds the bench's time; --accuracy-only with --accuracy-members 2 gives the wider ensemble)
-        accuracy = accuracy_report(members=1)
+        # mixed vs FP64 over the whole configured run of every workload: two perturbed FP64 runs
+        # for the chaotic collisions and compaction, one for the long settling runs (their FP64 runs
+        # dominate the bench's time); --accuracy-only with --accuracy-members sets any size
+        accuracy = accuracy_report(members={0: 2, 1: 1, 2: 1, 3: 2, 4: 2})
     adjoint = None if a.no_adjoint else adjoint_bench()
     packing_line = None if a.no_packing else packing_bench()
     bonds_line = None if a.no_packing else bonds_bench()

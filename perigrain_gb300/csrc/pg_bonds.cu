@@ -31,13 +31,40 @@ struct BondGrid {
   uint32_t dims[3];
 };
 
-__global__ void kb_box(const double* pos, uint32_t n, uint32_t dim, unsigned long long* box) {
+// Bounding box of the positions as ordered keys: each block folds its nodes with warp reductions
+// and shared memory, then one atomic per block and bound (a per-thread atomic on the same six words
+// serialised in L2: 54 us for 20k nodes).
+__global__ void __launch_bounds__(BT) kb_box(const double* pos, uint32_t n, uint32_t dim, unsigned long long* box) {
+  __shared__ unsigned long long red[6][BT / 32];
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  for (uint32_t c = 0; c < dim; ++c) {
-    const unsigned long long k = dbl_to_ordered(pos[(size_t)i * dim + c]);
-    atomicMin(&box[c], k);
-    atomicMax(&box[3 + c], k);
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  unsigned long long mn[3], mx[3];
+  for (uint32_t c = 0; c < 3; ++c) {
+    mn[c] = ~0ull;
+    mx[c] = 0ull;
+    if (c < dim && i < n) {
+      mn[c] = dbl_to_ordered(pos[(size_t)i * dim + c]);
+      mx[c] = mn[c];
+    }
+    mn[c] = warp_min_u64(mn[c]);
+    mx[c] = warp_max_u64(mx[c]);
+  }
+  if (lane == 0)
+    for (uint32_t c = 0; c < 3; ++c) {
+      red[c][warp] = mn[c];
+      red[3 + c][warp] = mx[c];
+    }
+  __syncthreads();
+  if (warp == 0) {
+    const uint32_t nw = blockDim.x >> 5;
+    for (uint32_t c = 0; c < dim; ++c) {
+      const unsigned long long a = warp_min_u64(lane < nw ? red[c][lane] : ~0ull);
+      const unsigned long long b = warp_max_u64(lane < nw ? red[3 + c][lane] : 0ull);
+      if (lane == 0) {
+        atomicMin(&box[c], a);
+        atomicMax(&box[3 + c], b);
+      }
+    }
   }
 }
 

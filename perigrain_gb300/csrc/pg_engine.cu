@@ -161,12 +161,17 @@ __global__ void k_mixed_images(const Dev P) {
 static int mixed_setup(pg_handle* h, const pg_setup_desc* s) {
   Dev& P = h->P;
   const uint32_t N = P.N, D = h->dim, SF = (D == 2) ? 2 : 4;
-  CU(h->dalloc(&P.bref, (size_t)N * 4 * D));
+  // bref and vol_f padded to whole warp chunks: the mixed force kernel's lanes past the last node
+  // gather their own (padding) index for bonds they never use
+  const size_t NP = (size_t)P.n_chunks * 32;
+  CU(h->dalloc(&P.bref, (NP - N) * 8 + (size_t)N * 4 * D));
   CU(h->dalloc(&P.cur_hl, (size_t)N * 2 * SF));
   CU(h->dalloc(&P.acc_f, (size_t)N * SF));
   CU(h->dalloc(&P.force_f, (size_t)N * SF));
   CU(h->dalloc(&P.extf_f, (size_t)N * SF));
-  CU(h->dalloc(&P.vol_f, N));
+  CU(h->dalloc(&P.vol_f, NP));
+  CU(cudaMemset(P.bref, 0, ((NP - N) * 8 + (size_t)N * 4 * D) * 4));
+  CU(cudaMemset(P.vol_f, 0, NP * 4));
   P.dt_f = (float)P.dt;
   P.hdt2_f = (float)P.hdt2;
   P.half_dt_f = (float)P.half_dt;

@@ -391,10 +391,10 @@ __global__ void __launch_bounds__(128) k_force_mx(const Dev P) {
       }
     }
     // the alive words and neighbour indices of the next pair are loaded one iteration ahead, so
-    // only the neighbour gathers wait on memory in each iteration. A lane without a node (the last
-    // chunk, d >= N) gathers node 0 for the bonds it never uses, never an index past the arrays.
-    const uint32_t dself = act ? d : 0u;
-    uint32_t wa_n = 0u, wb_n = 0u, ca_n = dself, cb_n = dself;
+    // only the neighbour gathers wait on memory in each iteration. A lane past the last node (d >= N
+    // in the last chunk) gathers its own index for bonds it never uses: bref and vol_f are allocated
+    // in whole chunks (zero padding), so those reads stay inside the arrays.
+    uint32_t wa_n = 0u, wb_n = 0u, ca_n = d, cb_n = d;
     if (cdeg > 0) {
       wa_n = P.alive[w0];
       ca_n = P.bcol[slot0];
@@ -415,13 +415,13 @@ __global__ void __launch_bounds__(128) k_force_mx(const Dev P) {
         cb_n = P.bcol[slot0 + 32u * (k + 3)];
       } else {
         wb_n = 0u;
-        cb_n = dself;
+        cb_n = d;
       }
       bool ba = (wa >> lane) & 1u, bb = (wb >> lane) & 1u;
       const bool ua = mov && ba, ub = mov && bb;
       const uint32_t sa = slot0 + 32u * k, sb = sa + 32u;
-      const uint32_t ja = ua ? ca : dself;
-      const uint32_t jb = ub ? cb : dself;
+      const uint32_t ja = ua ? ca : d;
+      const uint32_t jb = ub ? cb : d;
       float adh[D], adl[D], axh[D], axl[D], bdh[D], bdl[D], bxh[D], bxl[D];
       ld_ref<D>(P.bref, P.N, ja, adh, adl, axh, axl);
       ld_ref<D>(P.bref, P.N, jb, bdh, bdl, bxh, bxl);
