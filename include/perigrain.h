@@ -127,7 +127,26 @@ typedef struct pg_config {
                               (timeloop.h:1018-1369): gait clamps of local nodes 0-3, external
                               force in the first of three 1000-step phases only, contact and walls
                               for every movable grain (no stoppable gate), no torque or ramp */
+  int32_t node_order;      /* device layout of the nodes inside each grain (pg_node_order); results
+                              do not depend on it: the reference's orders -- bond rows, contact
+                              candidates, wall reactions, sums over a grain -- are kept through the
+                              nodes' original indices, and every output is in the input's order */
 } pg_config;
+
+/* Node layout inside each grain on the device. */
+typedef enum pg_node_order {
+  PG_ORDER_INPUT = 0,   /* as given */
+  PG_ORDER_CELL = 1,    /* default: cell-sorted -- strips of one node spacing (sqrt / cbrt of the
+                           mean node volume) along y (2D) or z then y (3D), x ascending within a
+                           strip, so that consecutive nodes (a warp's 32) are neighbours in space
+                           whatever order the mesh generator wrote them in. A grain whose input
+                           order is about as local already (mean index distance of bonded nodes
+                           at most 1.5x the cell order's) keeps its input order */
+  PG_ORDER_CELL_DEGREE = 2, /* the cell order's choice, then a stable sort by bond count (most
+                           bonds first), so warp chunks of the bond slab hold nodes of equal degree
+                           (less padding, less coalesced neighbour gathers: the autotuner decides) */
+  PG_ORDER_SHUFFLE = 3  /* a seeded random order (tests of the order independence) */
+} pg_node_order;
 
 /* ---- lifecycle ---------------------------------------------------------------------------- */
 int pg_version(void);
@@ -230,6 +249,9 @@ int pg_debug_grid_barrier(pg_handle* h, uint32_t arrivals);
 int pg_get_launch_config(pg_handle* h, uint32_t* block_size, uint32_t* cells_per_node);
 /* Contact candidate-list skin in use (fraction of R_c; 0: grid search every step). */
 int pg_get_contact_skin(pg_handle* h, double* skin);
+/* Node layout in use: the pg_node_order asked for (after autotuning), and whether it differs from
+ * the input's order (0: the input already was in that order, or PG_ORDER_INPUT). */
+int pg_get_node_order(pg_handle* h, int32_t* order, int32_t* permuted);
 /* Number of kernel launches issued by the last pg_step call. */
 int pg_get_launch_count(pg_handle* h, uint64_t* launches);
 /* Per-kernel device time of the last pg_step call (CUDA events; needs timing enabled). */

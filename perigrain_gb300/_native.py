@@ -44,9 +44,11 @@ class Config(C.Structure):
         ("precision", C.c_int32), ("record_pairs", C.c_int32), ("pair_log_capacity", C.c_uint32),
         ("first_step", C.c_uint32), ("max_contacts", C.c_uint32), ("block_size", C.c_uint32),
         ("autotune", C.c_int32), ("cells_per_node", C.c_uint32), ("contact_skin", C.c_double),
-        ("timeloop", C.c_int32),
+        ("timeloop", C.c_int32), ("node_order", C.c_int32),
     ]
 
+
+NODE_ORDER = {"input": 0, "cell": 1, "cell_degree": 2, "shuffle": 3}
 
 CONF_FIELDS = [
     ("timesteps", C.c_uint32), ("modulo", C.c_uint32), ("dt", C.c_double),
@@ -123,6 +125,7 @@ PROTOTYPES = [
     ("pg_get_launch_count", C.c_int, [C.c_void_p, u64p]),
     ("pg_get_launch_config", C.c_int, [C.c_void_p, u32p, u32p]),
     ("pg_get_contact_skin", C.c_int, [C.c_void_p, f64p]),
+    ("pg_get_node_order", C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     ("pg_set_timing", C.c_int, [C.c_void_p, C.c_int32]),
     ("pg_get_kernel_times", C.c_int, [C.c_void_p, f64p, f64p, u64p]),
     ("pg_build_bonds", C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_double, C.c_void_p, C.c_uint64, u64p,

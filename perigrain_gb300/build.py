@@ -25,7 +25,7 @@ BIN = os.path.join(HERE, "bin")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["pg_kernels.cu", "pg_kernels_mixed.cu", "pg_engine.cu", "pg_snapshot.cu", "pg_bonds.cu", "pg_noalloc.cu",
               "pg_adjoint.cu", "pg_adjoint_rev.cu", "pg_grad.cu", "pg_post.cu", "pg_pack.cu"]
-CXX_SOURCES = ["h5lite.cpp", "pg_io.cpp"]
+CXX_SOURCES = ["h5lite.cpp", "pg_io.cpp", "pg_order.cpp"]
 
 
 def _nvcc():

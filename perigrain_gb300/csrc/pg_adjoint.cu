@@ -289,7 +289,8 @@ __global__ void k_rp_reaction(const Dev P, const ReplayStep R) {
   const InstDev& in = P.inst[inst];
   const int dir = (D == 2) ? ((side == 0 || side == 1) ? 0 : 1) : (int)(side % 3);
   double r[3] = {0.0, 0.0, 0.0};
-  for (uint32_t d = in.node_begin; d < in.node_end; ++d) {
+  for (uint32_t o = in.node_begin; o < in.node_end; ++o) {  // the input's node order
+    const uint32_t d = at_of(P, o);
     const double* wo = R.wall_out + ((size_t)d * NS + side) * 4;
     if (wo[0] == 0.0 && wo[1] == 0.0 && wo[2] == 0.0 && wo[3] == 0.0) continue;
     r[dir] = r[dir] - wo[0];

@@ -576,8 +576,10 @@ __global__ void __launch_bounds__(256) k_grad_reduce(const Dev P, const double* 
   const uint32_t g = blockIdx.x;
   const GrainDev& gr = P.grain[g];
   double s[NPARAM] = {0.0, 0.0, 0.0, 0.0};
-  for (uint32_t i = gr.node_begin + threadIdx.x; i < gr.node_end; i += blockDim.x)
+  for (uint32_t o = gr.node_begin + threadIdx.x; o < gr.node_end; o += blockDim.x) {  // input order
+    const uint32_t i = at_of(P, o);
     for (int k = 0; k < NPARAM; ++k) s[k] += pacc[(size_t)i * NPARAM + k];
+  }
   for (int k = 0; k < NPARAM; ++k) sm[k][threadIdx.x] = s[k];
   __syncthreads();
   for (uint32_t w = blockDim.x / 2; w > 0; w >>= 1) {

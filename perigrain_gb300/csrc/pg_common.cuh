@@ -280,7 +280,7 @@ __device__ __forceinline__ void scatter_node(const Dev& P, uint32_t d) {
   P.sorted[at] = d;
   if (P.sorted_key) {
     const uint32_t g = P.node_grain[d];
-    const uint32_t sub = P.nl_bdry_only ? P.bdry_rank[d] : (d - P.grain[g].node_begin);
+    const uint32_t sub = P.nl_bdry_only ? P.bdry_rank[d] : (orig_of(P, d) - P.grain[g].node_begin);
     P.sorted_key[at] = ((unsigned long long)g << 32) | sub;
     if (P.dim == 2) {
       reinterpret_cast<float2*>(P.sorted_pos)[at] = reinterpret_cast<const float2*>(P.curf)[d];
@@ -308,9 +308,9 @@ static __global__ void k_torque_center(const Dev P) {
   const GrainDev gr = P.grain[g];
   double m[D];
   for (int c = 0; c < D; ++c) m[c] = 0.0;
-  for (uint32_t i = gr.node_begin; i < gr.node_end; ++i) {
+  for (uint32_t o = gr.node_begin; o < gr.node_end; ++o) {  // the input's node order
     double cu[D];
-    ldv<D>(P.cur, i, cu);
+    ldv<D>(P.cur, at_of(P, o), cu);
     for (int c = 0; c < D; ++c) m[c] = m[c] + cu[c];
   }
   double n = (double)(gr.node_end - gr.node_begin);

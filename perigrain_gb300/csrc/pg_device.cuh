@@ -151,6 +151,11 @@ struct Dev {
   double *xpos, *pos, *disp, *cur, *vel_in, *vel_out, *acc, *force, *extf, *vol;
   float* curf;  // float copy of (cur - origin) for the grid, stride SF
   uint32_t *node_grain, *bdry_rank;
+  // node layout (pg_config::node_order): node_orig[d] = the input's global index of device node d,
+  // node_at[o] = the device node of input node o; both null when the layout is the input order.
+  // The reference's orders are kept through them: candidate visit order and wall-reaction order by
+  // input index, the pair-log hash of input indices, sums over a grain in input order.
+  uint32_t *node_orig, *node_at;
   uint8_t *clamped, *clamp_pending;
   // grid
   uint32_t *cell_key, *cell_rank, *cell_count, *cell_start, *sorted;
@@ -266,6 +271,10 @@ __host__ __device__ inline double ordered_to_dbl(unsigned long long k) {
 // Gait phase of run_timeloop_worm at step t (timeloop.h:1097-1107): 0 in the first of every three
 // 1000-step periods (front nodes 0 and 3 held, external force on), 1 otherwise (back nodes 1, 2).
 __host__ __device__ inline uint32_t worm_phase(uint32_t t) { return ((t / 1000u) % 3u == 0u) ? 0u : 1u; }
+
+// The input's index of device node d, and the device node of input node o.
+__host__ __device__ inline uint32_t orig_of(const Dev& P, uint32_t d) { return P.node_orig ? P.node_orig[d] : d; }
+__host__ __device__ inline uint32_t at_of(const Dev& P, uint32_t o) { return P.node_at ? P.node_at[o] : o; }
 
 __host__ __device__ inline uint64_t splitmix64(uint64_t x) {
   x += 0x9e3779b97f4a7c15ull;

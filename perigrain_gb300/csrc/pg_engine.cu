@@ -15,6 +15,7 @@
 
 #include "pg_device.cuh"
 #include "pg_handle.h"
+#include "pg_order.h"
 #include "pg_kernels.h"
 #include "pg_kernels_mixed.h"
 
@@ -237,6 +238,7 @@ void pg_config_default(pg_config* c) {
   c->first_step = 1;
   c->max_contacts = 48;
   c->contact_skin = 0.25;
+  c->node_order = PG_ORDER_CELL;
 }
 
 // Host validation of a setup. With bonds_on_host the bond rows are checked here too (offsets
@@ -302,8 +304,8 @@ static int create_impl(const pg_setup_desc* s, const pg_config* cfg_in, pg_handl
 
 // The project's autotuner: every (force-kernel block size, grid cells per node) candidate runs
 // on a trial handle built from the same setup -- 3 warm-up steps, then 12 steps timed with CUDA
-// events on the handle's stream -- and the fastest is kept. The real handle starts from the
-// untouched setup.
+// events on the handle's stream -- and the fastest is kept; then the candidate-list skin and the
+// node layout, each by the same kind of trial. The real handle starts from the untouched setup.
 int pg_create(const pg_setup_desc* s, const pg_config* cfg_in, pg_handle** out) {
   if (!out || !cfg_in) return fail(PG_EINVAL, "null argument");
   if (!cfg_in->autotune) return create_impl(s, cfg_in, out);
@@ -359,11 +361,40 @@ int pg_create(const pg_setup_desc* s, const pg_config* cfg_in, pg_handle** out) 
       }
     }
   }
+  // third stage: the node layout inside the grains, cell order or cell order grouped by bond count
+  // (fewer padded slots in the bond slab, less coalesced neighbour gathers)
+  int32_t best_order = cfg_in->node_order;
+  if (cfg_in->node_order == PG_ORDER_CELL || cfg_in->node_order == PG_ORDER_CELL_DEGREE) {
+    const int32_t orders[] = {PG_ORDER_CELL, PG_ORDER_CELL_DEGREE};
+    double best_order_ms = 1e300;
+    for (int32_t od : orders) {
+      pg_config c = *cfg_in;
+      c.autotune = 0;
+      c.block_size = best_b;
+      c.cells_per_node = best_c;
+      c.contact_skin = best_skin;
+      c.node_order = od;
+      c.record_pairs = 0;
+      pg_handle* t = nullptr;
+      int rc = create_impl(s, &c, &t);
+      if (rc) return rc;
+      double ms = 0;
+      rc = pg_step(t, 3);
+      if (!rc) rc = pg_step_timed(t, 24, &ms);
+      pg_destroy(t);
+      if (rc) return rc;
+      if (ms < best_order_ms) {
+        best_order_ms = ms;
+        best_order = od;
+      }
+    }
+  }
   pg_config c = *cfg_in;
   c.autotune = 0;
   c.block_size = best_b;
   c.cells_per_node = best_c;
   c.contact_skin = best_skin;
+  c.node_order = best_order;
   return create_impl(s, &c, out);
 }
 
@@ -408,10 +439,14 @@ __global__ void k_check_bonds(const uint64_t* off, const uint32_t* loc, const ui
 __global__ void k_layout_bonds(const double* pos, uint32_t S, uint32_t D, uint32_t N, const uint64_t* off,
                                const uint32_t* loc, const uint32_t* grain_node_offset, const uint32_t* node_grain,
                                const uint32_t* chunk_slot, const uint32_t* chunk_word, const uint32_t* chunk_deg,
-                               uint32_t* bcol, double* bxin, uint32_t* alive) {
+                               const uint32_t* node_orig, const uint32_t* node_at, uint32_t* bcol, double* bxin,
+                               uint32_t* alive) {
   const uint32_t c = blockIdx.x, lane = threadIdx.x, i = c * 32 + lane;
   const bool act = i < N;
-  const uint32_t deg = act ? (uint32_t)(off[i + 1] - off[i]) : 0u;
+  // the row of device node i is the input's row of node_orig[i] (same grain), in its entry order;
+  // neighbours are renumbered into the layout through node_at
+  const uint32_t o = (act && node_orig) ? node_orig[i] : i;
+  const uint32_t deg = act ? (uint32_t)(off[o + 1] - off[o]) : 0u;
   const uint32_t n0 = act ? grain_node_offset[node_grain[i]] : 0u;
   const uint32_t cd = chunk_deg[c];
   for (uint32_t k = 0; k < cd; ++k) {
@@ -420,7 +455,8 @@ __global__ void k_layout_bonds(const double* pos, uint32_t S, uint32_t D, uint32
     uint32_t j = 0;
     double xn = 1.0;
     if (has) {
-      j = n0 + loc[off[i] + k];
+      j = n0 + loc[off[o] + k];
+      if (node_at) j = node_at[j];
       double xi[3] = {0.0, 0.0, 0.0};
       for (uint32_t a = 0; a < D; ++a) xi[a] = pos[(size_t)j * S + a] - pos[(size_t)i * S + a];
       double n2 = xi[0] * xi[0];
@@ -459,6 +495,15 @@ static int create_impl(const pg_setup_desc* s, const pg_config* cfg_in, pg_handl
   if (rc) return rc;
   tr.mark("validate");
   if (!have_dev) return fail(PG_ENODEV, "no CUDA device");
+  // node layout inside the grains (the device arrays follow `ord.perm`; outputs map back)
+  NodeOrder ord;
+  {
+    std::string err;
+    rc = make_node_order(s, cfg.node_order, &ord, &err);
+    if (rc) return fail(rc, err);
+  }
+  const bool permuted = !ord.perm.empty();
+  tr.mark("node order");
   if (cfg.pair_log_capacity == 0) cfg.pair_log_capacity = 1024;
   if (cfg.max_contacts == 0) cfg.max_contacts = 48;
   if (cfg.max_contacts > (uint32_t)MAX_CAND) cfg.max_contacts = MAX_CAND;
@@ -503,12 +548,23 @@ static int create_impl(const pg_setup_desc* s, const pg_config* cfg_in, pg_handl
   h->grain_node_offset.assign(s->grain_node_offset, s->grain_node_offset + G + 1);
   h->bond_offset.assign(s->bond_offset, s->bond_offset + N + 1);
 
-  // ---- node arrays (reference order; stride S) ----
+  h->node_order = cfg.node_order;
+  if (permuted) {
+    h->node_orig = ord.perm;
+    CU(h->dalloc(&P.node_orig, N));
+    CU(h->dalloc(&P.node_at, N));
+    CU(cudaMemcpy(P.node_orig, ord.perm.data(), (size_t)N * 4, cudaMemcpyHostToDevice));
+    CU(cudaMemcpy(P.node_at, ord.at.data(), (size_t)N * 4, cudaMemcpyHostToDevice));
+  }
+
+  // ---- node arrays (the layout's order; stride S) ----
   std::vector<double> tmp((size_t)N * S, 0.0);
   auto pack = [&](const double* src) {
     std::fill(tmp.begin(), tmp.end(), 0.0);
-    for (uint32_t i = 0; i < N; ++i)
-      for (uint32_t c = 0; c < D; ++c) tmp[(size_t)i * S + c] = src[(size_t)i * D + c];
+    for (uint32_t i = 0; i < N; ++i) {
+      const size_t o = permuted ? ord.perm[i] : i;
+      for (uint32_t c = 0; c < D; ++c) tmp[(size_t)i * S + c] = src[o * D + c];
+    }
   };
   double** vecs[] = {&P.pos, &P.disp, &P.cur, &h->vel_a, &h->vel_b, &P.acc, &P.force, &P.extf};
   for (double** v : vecs) CU(h->dalloc(v, (size_t)N * S));
@@ -517,7 +573,7 @@ static int create_impl(const pg_setup_desc* s, const pg_config* cfg_in, pg_handl
   CU(h->dalloc(&P.curf, (size_t)N * S));
   // in 2D the stride is the dimension: straight uploads; in 3D through the padded host buffer
   auto upload = [&](double* dst, const double* src) -> cudaError_t {
-    if (S == D) return cudaMemcpy(dst, src, (size_t)N * D * 8, cudaMemcpyHostToDevice);
+    if (S == D && !permuted) return cudaMemcpy(dst, src, (size_t)N * D * 8, cudaMemcpyHostToDevice);
     pack(src);
     return cudaMemcpy(dst, tmp.data(), tmp.size() * 8, cudaMemcpyHostToDevice);
   };
@@ -533,21 +589,29 @@ static int create_impl(const pg_setup_desc* s, const pg_config* cfg_in, pg_handl
     k_add_vec<<<(N * S + 255) / 256, 256>>>(P.pos, P.disp, P.cur, N * S);
     CU(cudaGetLastError());
   }
-  CU(cudaMemcpy(P.vol, s->vol, (size_t)N * 8, cudaMemcpyHostToDevice));
+  if (permuted) {
+    std::vector<double> v(N);
+    for (uint32_t i = 0; i < N; ++i) v[i] = s->vol[ord.perm[i]];
+    CU(cudaMemcpy(P.vol, v.data(), (size_t)N * 8, cudaMemcpyHostToDevice));
+  } else {
+    CU(cudaMemcpy(P.vol, s->vol, (size_t)N * 8, cudaMemcpyHostToDevice));
+  }
   tr.mark("node vectors");
 
   // ---- per node metadata ----
   std::vector<uint32_t> node_grain(N), bdry_rank(N, NONE);
   std::vector<uint8_t> clamped(N, 0);
+  const uint32_t* bdry_nodes = permuted ? ord.bdry_nodes.data() : s->bdry_nodes;
+  const uint32_t* clamped_nodes = permuted ? ord.clamped_nodes.data() : s->clamped_nodes;
   for (uint32_t g = 0; g < G; ++g) {
     uint32_t n0 = s->grain_node_offset[g];
     for (uint32_t i = n0; i < s->grain_node_offset[g + 1]; ++i) node_grain[i] = g;
     for (uint32_t k = s->bdry_offset[g]; k < s->bdry_offset[g + 1]; ++k) {
-      uint32_t nd = n0 + s->bdry_nodes[k];
+      uint32_t nd = n0 + bdry_nodes[k];
       if (bdry_rank[nd] != NONE) return fail(PG_EINVAL, "duplicate entry in bdry_nodes of grain " + std::to_string(g));
       bdry_rank[nd] = k - s->bdry_offset[g];
     }
-    for (uint32_t k = s->clamped_offset[g]; k < s->clamped_offset[g + 1]; ++k) clamped[n0 + s->clamped_nodes[k]] = 1;
+    for (uint32_t k = s->clamped_offset[g]; k < s->clamped_offset[g + 1]; ++k) clamped[n0 + clamped_nodes[k]] = 1;
   }
   CU(h->dalloc(&P.node_grain, N));
   CU(h->dalloc(&P.bdry_rank, N));
@@ -567,7 +631,10 @@ static int create_impl(const pg_setup_desc* s, const pg_config* cfg_in, pg_handl
   std::vector<uint32_t> chunk_deg(NC, 0);
   for (uint32_t i = 0; i < N; ++i) {
     if (s->bond_offset[i + 1] < s->bond_offset[i]) return fail(PG_EINVAL, "bond_offset decreasing");
-    h->node_deg[i] = (uint32_t)(s->bond_offset[i + 1] - s->bond_offset[i]);
+  }
+  for (uint32_t i = 0; i < N; ++i) {
+    const uint32_t o = permuted ? ord.perm[i] : i;
+    h->node_deg[i] = (uint32_t)(s->bond_offset[o + 1] - s->bond_offset[o]);
     chunk_deg[i >> 5] = std::max<uint32_t>(chunk_deg[i >> 5], h->node_deg[i]);
   }
   uint64_t slots = 0, words = 0;
@@ -625,7 +692,7 @@ static int create_impl(const pg_setup_desc* s, const pg_config* cfg_in, pg_handl
     }
     if (e == cudaSuccess) {
       k_layout_bonds<<<NC, 32>>>(P.pos, S, D, N, d_off, d_loc, d_gno, P.node_grain, P.chunk_slot, P.chunk_word,
-                                 P.chunk_deg, P.bcol, P.bxin, P.alive);
+                                 P.chunk_deg, P.node_orig, P.node_at, P.bcol, P.bxin, P.alive);
       e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaMemset(P.break_step, 0, slots * 4);
@@ -960,25 +1027,33 @@ int pg_get_field(pg_handle* h, int field, double* out) {
       k_widen_field<<<(N * D + 255) / 256, 256, 0, h->stream>>>(
           field == PG_FIELD_ACC ? h->P.acc_f : h->P.force_f, S, D, N, h->field_scratch);
       CU(cudaGetLastError());
-      CU(cudaMemcpyAsync(out, h->field_scratch, (size_t)N * D * 8, cudaMemcpyDeviceToHost, h->stream));
-      CU(cudaStreamSynchronize(h->stream));
+      if (h->node_orig.empty()) {
+        CU(cudaMemcpyAsync(out, h->field_scratch, (size_t)N * D * 8, cudaMemcpyDeviceToHost, h->stream));
+        CU(cudaStreamSynchronize(h->stream));
+      } else {
+        std::vector<double> tmp((size_t)N * D);
+        CU(cudaMemcpyAsync(tmp.data(), h->field_scratch, tmp.size() * 8, cudaMemcpyDeviceToHost, h->stream));
+        CU(cudaStreamSynchronize(h->stream));
+        for (uint32_t i = 0; i < N; ++i)
+          for (uint32_t c = 0; c < D; ++c) out[(size_t)h->node_orig[i] * D + c] = tmp[(size_t)i * D + c];
+      }
     }
     return PG_OK;
   }
-  if (S == D) {
+  if (S == D && h->node_orig.empty()) {
     CU(cudaMemcpy(out, src, (size_t)N * D * 8, cudaMemcpyDeviceToHost));
   } else {
     std::vector<double> tmp((size_t)N * S);
     CU(cudaMemcpy(tmp.data(), src, tmp.size() * 8, cudaMemcpyDeviceToHost));
     for (uint32_t i = 0; i < N; ++i)
-      for (uint32_t c = 0; c < D; ++c) out[(size_t)i * D + c] = tmp[(size_t)i * S + c];
+      for (uint32_t c = 0; c < D; ++c) out[(size_t)h->orig(i) * D + c] = tmp[(size_t)i * S + c];
   }
   if (field == PG_FIELD_DISP) {
     std::vector<uint8_t> pend(N);
     CU(cudaMemcpy(pend.data(), h->P.clamp_pending, N, cudaMemcpyDeviceToHost));
     for (uint32_t i = 0; i < N; ++i)
       if (pend[i])
-        for (uint32_t c = 0; c < D; ++c) out[(size_t)i * D + c] = 0.0;
+        for (uint32_t c = 0; c < D; ++c) out[(size_t)h->orig(i) * D + c] = 0.0;
   }
   return PG_OK;
 }
@@ -988,6 +1063,14 @@ int pg_set_field(pg_handle* h, int field, const double* in) {
   int rc = pg_synchronize(h);
   if (rc) return rc;
   const uint32_t N = h->P.N, D = h->dim, S = h->S;
+  // the values in the layout's node order
+  std::vector<double> in_layout;
+  if (!h->node_orig.empty()) {
+    in_layout.resize((size_t)N * D);
+    for (uint32_t i = 0; i < N; ++i)
+      for (uint32_t c = 0; c < D; ++c) in_layout[(size_t)i * D + c] = in[(size_t)h->node_orig[i] * D + c];
+    in = in_layout.data();
+  }
   if (field == PG_FIELD_POS && !h->xpos_separate) {
     // keep the bond reference positions (xi = pos[j] - pos[i] at load time) unchanged
     double* x = nullptr;
@@ -1050,7 +1133,7 @@ int pg_get_bond_alive(pg_handle* h, uint8_t* out) {
   for (uint32_t i = 0; i < N; ++i) {
     const uint32_t c = i >> 5, lane = i & 31;
     for (uint32_t k = 0; k < h->node_deg[i]; ++k)
-      out[h->bond_offset[i] + k] = (words[h->chunk_word[c] + k] >> lane) & 1u;
+      out[h->bond_offset[h->orig(i)] + k] = (words[h->chunk_word[c] + k] >> lane) & 1u;
   }
   return PG_OK;
 }
@@ -1065,7 +1148,7 @@ int pg_get_bond_break_step(pg_handle* h, uint32_t* out) {
   for (uint32_t i = 0; i < N; ++i) {
     const uint32_t c = i >> 5, lane = i & 31;
     for (uint32_t k = 0; k < h->node_deg[i]; ++k)
-      out[h->bond_offset[i] + k] = bs[h->chunk_slot[c] + (size_t)k * 32 + lane];
+      out[h->bond_offset[h->orig(i)] + k] = bs[h->chunk_slot[c] + (size_t)k * 32 + lane];
   }
   return PG_OK;
 }
@@ -1079,7 +1162,7 @@ int pg_set_bond_alive(pg_handle* h, const uint8_t* in) {
   for (uint32_t i = 0; i < N; ++i) {
     const uint32_t c = i >> 5, lane = i & 31;
     for (uint32_t k = 0; k < h->node_deg[i]; ++k)
-      if (in[h->bond_offset[i] + k]) words[h->chunk_word[c] + k] |= 1u << lane;
+      if (in[h->bond_offset[h->orig(i)] + k]) words[h->chunk_word[c] + k] |= 1u << lane;
   }
   if (!words.empty()) CU(cudaMemcpy(h->P.alive, words.data(), words.size() * 4, cudaMemcpyHostToDevice));
   return PG_OK;
@@ -1178,6 +1261,13 @@ int pg_get_launch_config(pg_handle* h, uint32_t* block_size, uint32_t* cells_per
   if (!h) return fail(PG_EINVAL, "null handle");
   if (block_size) *block_size = h->L.force_block;
   if (cells_per_node) *cells_per_node = h->L.cells_per_node;
+  return PG_OK;
+}
+
+int pg_get_node_order(pg_handle* h, int32_t* order, int32_t* permuted) {
+  if (!h) return fail(PG_EINVAL, "null handle");
+  if (order) *order = h->node_order;
+  if (permuted) *permuted = h->node_orig.empty() ? 0 : 1;
   return PG_OK;
 }
 

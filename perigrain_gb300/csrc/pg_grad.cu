@@ -555,7 +555,7 @@ int pg_grad_backward(pg_handle* h, const double* disp_bar, const double* vel_bar
     std::fill(tmp.begin(), tmp.end(), 0.0);
     if (src)
       for (size_t i = 0; i < N; ++i)
-        for (size_t c = 0; c < D; ++c) tmp[i * S + c] = src[i * D + c];
+        for (size_t c = 0; c < D; ++c) tmp[i * S + c] = src[(size_t)h->orig((uint32_t)i) * D + c];
     CU(cudaMemcpyAsync(dst, tmp.data(), tmp.size() * 8, cudaMemcpyHostToDevice, h->stream));
     CU(cudaStreamSynchronize(h->stream));
     return PG_OK;

@@ -171,6 +171,10 @@ struct pg_handle {
   bool xpos_separate = false;
   // set when a status check saw PG_ETIMEOUT (a bounded device wait ran out): pg_step refuses
   bool halted = false;
+  // node layout: node_orig[d] = the input's index of device node d (empty: input order)
+  std::vector<uint32_t> node_orig;
+  int32_t node_order = 0;  // pg_node_order asked for
+  uint32_t orig(uint32_t d) const { return node_orig.empty() ? d : node_orig[d]; }
   std::vector<void*> allocs;
   // host copies needed for mapping
   std::vector<uint64_t> bond_offset;  // reference CSR

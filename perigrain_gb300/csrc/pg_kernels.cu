@@ -229,7 +229,7 @@ __global__ void __launch_bounds__(128) k_force(const Dev P) {
         grain_box<D>(P, gq, qmn, qmx);
         if (!boxes_touch<D>(bmn, bmx, qmn, qmx, in.contact_rad)) return;
       }
-      const uint32_t sub = P.nl_bdry_only ? P.bdry_rank[q] : (q - P.grain[gq].node_begin);
+      const uint32_t sub = P.nl_bdry_only ? P.bdry_rank[q] : (orig_of(P, q) - P.grain[gq].node_begin);
       const unsigned long long key =
           ((unsigned long long)(same ? 0u : 1u) << 63) | ((unsigned long long)gq << 32) | sub;
       insert_cand<D>(keys, idx, nc, key, q, P);
@@ -294,7 +294,7 @@ __global__ void __launch_bounds__(128) k_force(const Dev P) {
       if (!(dn <= Rc)) continue;
       if (P.record_pairs) {
         my_pairs += 1;
-        my_hash += splitmix64(((unsigned long long)d << 32) | q);
+        my_hash += splitmix64(((unsigned long long)orig_of(P, d) << 32) | orig_of(P, q));
       }
       if (dn == 0.0) my_close += 1;
       double u[D];
@@ -382,7 +382,7 @@ __global__ void __launch_bounds__(128) k_force(const Dev P) {
         rec.a_t2 = 0;
         rec.a_damp = 0;
         // replay key: the reference sums reactions grain by grain in its node-loop order
-        rec.gid = P.nl_bdry_only ? (gr.node_begin + P.bdry_rank[d]) : d;
+        rec.gid = P.nl_bdry_only ? (gr.node_begin + P.bdry_rank[d]) : orig_of(P, d);
         rec.side = (uint16_t)side;
         rec.has_fric = 0;
         rec.has_damp = 0;
@@ -500,7 +500,7 @@ __global__ void __launch_bounds__(128) k_force(const Dev P) {
         }
         P.clamp_pending[d] = 1;
       }
-      if (P.worm) worm_clamp<D>(d - gr.node_begin, worm_phase(t), a, v);
+      if (P.worm) worm_clamp<D>(orig_of(P, d) - gr.node_begin, worm_phase(t), a, v);
       stv<D>(P.acc, d, a);
       stv<D>(P.vel_out, d, v);
     } else {

@@ -489,7 +489,7 @@ __global__ void __launch_bounds__(128) k_force_mx(const Dev P) {
         grain_box<D>(P, gq, qmn, qmx);
         if (!boxes_touch<D>(bmn, bmx, qmn, qmx, in.contact_rad)) return;
       }
-      const uint32_t sub = P.nl_bdry_only ? P.bdry_rank[q] : (q - P.grain[gq].node_begin);
+      const uint32_t sub = P.nl_bdry_only ? P.bdry_rank[q] : (orig_of(P, q) - P.grain[gq].node_begin);
       const unsigned long long key =
           ((unsigned long long)(same ? 0u : 1u) << 63) | ((unsigned long long)gq << 32) | sub;
       insert_cand<D>(keys, idx, nc, key, q, P);
@@ -565,7 +565,7 @@ __global__ void __launch_bounds__(128) k_force_mx(const Dev P) {
       for (int c = 0; c < D; ++c) dir[c] = (float)dir64[c];
       if (P.record_pairs) {
         my_pairs += 1;
-        my_hash += splitmix64(((unsigned long long)d << 32) | q);
+        my_hash += splitmix64(((unsigned long long)orig_of(P, d) << 32) | orig_of(P, q));
       }
       if (dn == 0.f) my_close += 1;
       const float inv = 1.f / dn;
@@ -647,7 +647,7 @@ __global__ void __launch_bounds__(128) k_force_mx(const Dev P) {
         rec.a_t1 = 0;
         rec.a_t2 = 0;
         rec.a_damp = 0;
-        rec.gid = P.nl_bdry_only ? (gr.node_begin + P.bdry_rank[d]) : d;
+        rec.gid = P.nl_bdry_only ? (gr.node_begin + P.bdry_rank[d]) : orig_of(P, d);
         rec.side = (uint16_t)side;
         rec.has_fric = 0;
         rec.has_damp = 0;
@@ -765,7 +765,7 @@ __global__ void __launch_bounds__(128) k_force_mx(const Dev P) {
         }
         P.clamp_pending[d] = 1;
       }
-      if (P.worm) worm_clamp<D>(d - gr.node_begin, worm_phase(t), a, v);
+      if (P.worm) worm_clamp<D>(orig_of(P, d) - gr.node_begin, worm_phase(t), a, v);
       stvf<D>(P.acc_f, d, a);
       stv<D>(P.vel_out, d, v);
     } else {

@@ -41,7 +41,8 @@ __global__ void __launch_bounds__(POST_THREADS) k_post(const Dev P, const double
   const bool mixed = P.acc_f != nullptr;
   double s[NQ];
   for (int k = 0; k < NQ; ++k) s[k] = 0.0;
-  for (uint32_t i = gr.node_begin + tid; i < gr.node_end; i += POST_THREADS) {
+  for (uint32_t o = gr.node_begin + tid; o < gr.node_end; o += POST_THREADS) {  // the input's order
+    const uint32_t i = at_of(P, o);
     double v[D], x[D], a[D], f[D];
     ldv<D>(vel, i, v);
     ldv<D>(P.cur, i, x);
@@ -68,7 +69,7 @@ __global__ void __launch_bounds__(POST_THREADS) k_post(const Dev P, const double
     uint32_t deg = 0;
     for (uint32_t k = 0; k < deg0; ++k) deg += (P.alive[P.chunk_word[c] + k] >> lane) & 1u;
     const double q = ((double)deg0 - (double)deg) / (double)deg0;  // 0/0 -> NaN, as numpy
-    if (node_damage) node_damage[i] = q;
+    if (node_damage) node_damage[o] = q;
     s[5 * D] += q;
     s[5 * D + 1] += vol;
     s[5 * D + 2] += 1.0;

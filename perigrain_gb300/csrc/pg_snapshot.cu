@@ -27,6 +27,7 @@ struct SnapArgs {
   int nf;
   int disp_slot;                 // slot of the displacement field (-1: none)
   const uint8_t* clamp_pending;  // nodes whose clamp is applied at the next step read 0 there
+  const uint32_t* node_at;       // device node of each input node (null: input order)
   uint32_t N, D, S;
   // bonds: alive bytes in CSR order
   const uint32_t *alive, *chunk_word, *node_deg;
@@ -54,7 +55,9 @@ __global__ void k_snap_gather(SnapArgs a) {
     const bool f32 = (a.is32 >> f) & 1u;
     const bool is_disp = f == a.disp_slot;
     for (size_t e = tid; e < ND; e += nth) {
-      const uint32_t i = (uint32_t)(e / a.D), c = (uint32_t)(e - (size_t)i * a.D);
+      // element e of the output is component c of input node e / D
+      const uint32_t o = (uint32_t)(e / a.D), c = (uint32_t)(e - (size_t)o * a.D);
+      const uint32_t i = a.node_at ? a.node_at[o] : o;
       const size_t si = (size_t)i * a.S + c;
       double v = f32 ? (double)static_cast<const float*>(a.src[f])[si] : static_cast<const double*>(a.src[f])[si];
       if (is_disp && a.clamp_pending[i]) v = 0.0;
@@ -62,10 +65,11 @@ __global__ void k_snap_gather(SnapArgs a) {
     }
   }
   if (a.alive_out) {
-    for (size_t i = tid; i < a.N; i += nth) {
+    for (size_t on = tid; on < a.N; on += nth) {  // input node on, in CSR order
+      const uint32_t i = a.node_at ? a.node_at[on] : (uint32_t)on;
       const uint32_t c = (uint32_t)(i >> 5), lane = (uint32_t)(i & 31);
       const uint32_t* w = a.alive + a.chunk_word[c];
-      uint8_t* o = a.alive_out + a.bond_offset[i];
+      uint8_t* o = a.alive_out + a.bond_offset[on];
       const uint32_t deg = a.node_deg[i];
       for (uint32_t k = 0; k < deg; ++k) o[k] = (uint8_t)((w[k] >> lane) & 1u);
     }
@@ -186,6 +190,7 @@ int pg_snapshot(pg_handle* h, const pg_snapshot_desc* d) {
   a.nf = nf;
   a.disp_slot = disp_slot;
   a.clamp_pending = h->P.clamp_pending;
+  a.node_at = h->P.node_at;
   a.N = N;
   a.D = D;
   a.S = h->S;

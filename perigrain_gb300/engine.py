@@ -19,7 +19,7 @@ class Simulation:
     def __init__(self, setup, dt, enable_fracture=1, nl_bdry_only=0, allow_damping=1, allow_friction=1,
                  self_contact=1, enable_torque=0, gradient_extforce=0, extforce_maxstep=0, precision="fp64",
                  record_pairs=False, pair_log_capacity=1024, first_step=1, max_contacts=48, block_size=0,
-                 autotune=False, cells_per_node=0, timeloop=0, contact_skin=0.25):
+                 autotune=False, cells_per_node=0, timeloop=0, contact_skin=0.25, node_order=None):
         L = N.lib()
         self.setup = setup
         self.dim = setup.dim
@@ -44,6 +44,8 @@ class Simulation:
         cfg.cells_per_node = int(cells_per_node)
         cfg.timeloop = 1 if timeloop in (1, "worm") else 0
         cfg.contact_skin = float(contact_skin)
+        if node_order is not None:
+            cfg.node_order = N.NODE_ORDER[node_order] if isinstance(node_order, str) else int(node_order)
         self.cfg = cfg
         self._desc = setup.desc()
         h = C.c_void_p()
@@ -209,6 +211,13 @@ class Simulation:
         tc = C.c_uint64()
         N.check(N.lib().pg_get_device_status(self.h, C.byref(st), C.byref(tc)))
         return st.value, tc.value
+
+    def node_order(self):
+        """(name of the node layout in use, whether it differs from the input's order)."""
+        o, p = C.c_int32(), C.c_int32()
+        N.check(N.lib().pg_get_node_order(self.h, C.byref(o), C.byref(p)))
+        names = {v: k for k, v in N.NODE_ORDER.items()}
+        return names.get(o.value, str(o.value)), bool(p.value)
 
     def contact_skin(self):
         """Candidate-list skin in use (fraction of R_c; 0: grid search every step)."""
