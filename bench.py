@@ -558,7 +558,7 @@ ACC_EPS = 2.0 ** -24  # FP32 unit round-off: size of the FP64 ensemble's velocit
 ACC_POS_TOL = 1e-6  # pointwise relative position error bound while the dynamics do not amplify
 # whole-run statistics: a mixed-vs-FP64 difference passes when it is at most max(2 x the FP64
 # ensemble's spread, floor); the floors are relative to the statistic's FP64 scale
-ACC_STAT_FLOOR = {"kinetic_energy": 2e-2, "mean_grain_speed": 5e-2, "grain_centroid": 2e-2,
+ACC_STAT_FLOOR = {"kinetic_energy": 2e-2, "mean_grain_speed": 5e-2, "grain_centroid": 5e-2,
                   "reaction_window_means": 5e-2, "broken_bonds": 1e-1}
 
 
@@ -713,8 +713,8 @@ def accuracy_report(configs=(0, 1, 2, 3, 4), members=2):
 ACCURACY_TOLERANCE = (
     "pointwise: relative position error <= 1e-6 up to the step given per workload (the dynamics then amplify "
     "any difference; later horizons are reported beside the FP64 ensemble spread); whole run: each statistic "
-    "differs from FP64 by at most max(2 x ensemble spread, floor) -- kinetic-energy series and grain centroids "
-    "(relative to the grains' travel) 2e-2, mean grain speed and windowed wall-reaction means 5e-2, broken-bond "
+    "differs from FP64 by at most max(2 x ensemble spread, floor) -- kinetic-energy series 2e-2; mean grain "
+    "speed, grain centroids (relative to the grains' travel) and windowed wall-reaction means 5e-2; broken-bond "
     "count 1e-1 (relative); momentum "
     "drift <= 1e-6 of sum(m|v0|) without walls")
 
@@ -833,7 +833,7 @@ def main():
     setup, spec = build_workload(a.workload, rank)
     kw = engine_kwargs(spec, a.precision)
     sim = Simulation(setup, autotune=not a.profile_run, **kw)
-    tuned = dict(sim.launch_config(), contact_skin=sim.contact_skin())
+    tuned = dict(sim.launch_config(), contact_skin=sim.contact_skin(), node_order=sim.node_order()[0])
     sim.step(a.warmup)
     sim.synchronize()
     if a.profile_run:

@@ -701,6 +701,40 @@ __device__ __forceinline__ bool grid_barrier(const Dev& P, uint32_t* ok_smem) {
   return *ok_smem != 0;
 }
 
+// SCAN_PER consecutive cell counts from `base` (a multiple of SCAN_PER): four 16-byte loads when the
+// run lies inside the table, element by element at its end (zeros past it).
+__device__ __forceinline__ void load_counts(const Dev& P, uint32_t base, uint32_t (&v)[SCAN_PER]) {
+  if (base + SCAN_PER <= P.table_total) {
+    const uint4* q4 = reinterpret_cast<const uint4*>(P.cell_count + base);
+    for (int k = 0; k < SCAN_PER / 4; ++k) {
+      const uint4 q = q4[k];
+      v[4 * k] = q.x;
+      v[4 * k + 1] = q.y;
+      v[4 * k + 2] = q.z;
+      v[4 * k + 3] = q.w;
+    }
+  } else {
+    for (int k = 0; k < SCAN_PER; ++k) v[k] = base + k < P.table_total ? P.cell_count[base + k] : 0u;
+  }
+}
+// Cell starts of the run at `base`, and its counts cleared for the next build.
+__device__ __forceinline__ void store_starts_clear_counts(const Dev& P, uint32_t base, const uint32_t (&st)[SCAN_PER]) {
+  if (base + SCAN_PER <= P.table_total) {
+    uint4* s4 = reinterpret_cast<uint4*>(P.cell_start + base);  // base is a multiple of 16 entries
+    uint4* z4 = reinterpret_cast<uint4*>(P.cell_count + base);
+    for (int k = 0; k < SCAN_PER / 4; ++k) {
+      s4[k] = make_uint4(st[4 * k], st[4 * k + 1], st[4 * k + 2], st[4 * k + 3]);
+      z4[k] = make_uint4(0u, 0u, 0u, 0u);
+    }
+  } else {
+    for (int k = 0; k < SCAN_PER; ++k)
+      if (base + k < P.table_total) {
+        P.cell_start[base + k] = st[k];
+        P.cell_count[base + k] = 0u;
+      }
+  }
+}
+
 template <int D>
 static __global__ void __launch_bounds__(SCAN_THREADS) k_grid_coop(const Dev P) {
   pdl_enter();
@@ -728,11 +762,9 @@ static __global__ void __launch_bounds__(SCAN_THREADS) k_grid_coop(const Dev P) 
   const uint32_t ntiles = cdiv_dev(P.table_total, SCAN_TILE);
   for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const uint32_t base = tile * SCAN_TILE + threadIdx.x * SCAN_PER;
-    uint32_t sum = 0;
-    for (int k = 0; k < SCAN_PER; ++k) {
-      const uint32_t i = base + k;
-      if (i < P.table_total) sum += P.cell_count[i];
-    }
+    uint32_t v[SCAN_PER], sum = 0;
+    load_counts(P, base, v);
+    for (int k = 0; k < SCAN_PER; ++k) sum += v[k];
     uint32_t tot;
     block_excl_scan(sum, ws, &tot);
     if (threadIdx.x == 0) P.scan_tile_sum[tile] = tot;
@@ -759,20 +791,15 @@ static __global__ void __launch_bounds__(SCAN_THREADS) k_grid_coop(const Dev P) 
   for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const uint32_t base = tile * SCAN_TILE + threadIdx.x * SCAN_PER;
     uint32_t v[SCAN_PER], sum = 0;
-    for (int k = 0; k < SCAN_PER; ++k) {
-      const uint32_t i = base + k;
-      v[k] = i < P.table_total ? P.cell_count[i] : 0;
-      sum += v[k];
-    }
+    load_counts(P, base, v);
+    for (int k = 0; k < SCAN_PER; ++k) sum += v[k];
     uint32_t ex = block_excl_scan(sum, ws, nullptr) + ((volatile uint32_t*)P.scan_tile_sum)[tile];
+    uint32_t st[SCAN_PER];
     for (int k = 0; k < SCAN_PER; ++k) {
-      const uint32_t i = base + k;
-      if (i < P.table_total) {
-        P.cell_start[i] = ex;
-        P.cell_count[i] = 0;
-      }
+      st[k] = ex;
       ex += v[k];
     }
+    store_starts_clear_counts(P, base, st);
     __syncthreads();
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) P.cell_start[P.table_total] = P.N;
