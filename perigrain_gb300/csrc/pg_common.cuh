@@ -280,7 +280,7 @@ __device__ __forceinline__ void scatter_node(const Dev& P, uint32_t d) {
   P.sorted[at] = d;
   if (P.sorted_key) {
     const uint32_t g = P.node_grain[d];
-    const uint32_t sub = P.nl_bdry_only ? P.bdry_rank[d] : (orig_of(P, d) - P.grain[g].node_begin);
+    const uint32_t sub = P.node_sub[d];
     P.sorted_key[at] = ((unsigned long long)g << 32) | sub;
     if (P.dim == 2) {
       reinterpret_cast<float2*>(P.sorted_pos)[at] = reinterpret_cast<const float2*>(P.curf)[d];

@@ -80,12 +80,16 @@ struct InstDev {
   float skin_lim2;      // candidate lists: squared displacement since the last build that forces
                         // a rebuild, (0.45 skin)^2 (the Verlet bound is skin/2; FP32 margin)
   uint32_t dims[3];     // cells per axis (dims[2] = 1 in 2D)
-  // rel_frame != 0 (mixed path with candidate lists): the FP32 position images (cur_hl, curf) are
+  // rel_frame != 0 (mixed path with candidate lists): the FP32 position images (curf) are
   // offsets from xorigin, which never moves, so the position update of a step does not depend on
   // the grid refit of the step before; frame_off_f = xorigin - origin turns them into offsets from
   // the grid origin for cell coordinates. Otherwise the images are offsets from origin, and 0.
   float frame_off_f[3];
   int32_t rel_frame;
+  // the images' origin in FP32 (xorigin with rel_frame, else this step's grid origin): an image is
+  // trunc_f32(CurrPos) - org_f, formed in FP32 (its error, ~1e-7 of the coordinates' size, is far
+  // inside the 1/16 margin of the prefilter radius and the cell edge)
+  float org_f[3];
   uint32_t table_off, table_cap;
   uint32_t node_begin, node_end, grain_begin, grain_end;
   int32_t allow_wall;
@@ -119,6 +123,7 @@ __host__ __device__ inline void fit_grid(InstDev& in, int D, const double* lo, c
     in.origin[a] = a < D ? lo[a] - 2.0 * (double)cs : 0.0;
     in.dims[a] = a < D ? n[a] : 1u;
     in.frame_off_f[a] = (in.rel_frame && a < D) ? (float)(in.xorigin[a] - in.origin[a]) : 0.f;
+    in.org_f[a] = a < D ? (float)(in.rel_frame ? in.xorigin[a] : in.origin[a]) : 0.f;
   }
 }
 
@@ -156,6 +161,10 @@ struct Dev {
   // The reference's orders are kept through them: candidate visit order and wall-reaction order by
   // input index, the pair-log hash of input indices, sums over a grain in input order.
   uint32_t *node_orig, *node_at;
+  // the low half of a node's candidate key in the reference's visit order: its rank in the
+  // grain's nonlocal boundary list with nl_bdry_only (NONE for other nodes), else its input index
+  // within its grain
+  uint32_t* node_sub;
   uint8_t *clamped, *clamp_pending;
   // grid
   uint32_t *cell_key, *cell_rank, *cell_count, *cell_start, *sorted;
@@ -225,9 +234,9 @@ struct Dev {
   // mixed precision (PG_MIXED): FP32 hi/lo pairs (x = hi + lo to ~2^-47 |x|). `bref` interleaves,
   // per node, the pair of the FP64 displacement and the pair of the bond reference position
   // (relative to the instance's fixed origin) -- 4*SF floats, one 32-byte sector in 2D -- so a bond
-  // gathers its neighbour's data from one sector. `cur_hl` holds CurrPos relative to the grid
-  // origin (2*SF floats). FP32 acceleration, force, external force and volume.
-  float *bref, *cur_hl;
+  // gathers its neighbour's data from one sector. FP32 acceleration, force, external force and
+  // volume.
+  float* bref;
   float *acc_f, *force_f, *extf_f, *vol_f;
   float dt_f, hdt2_f, half_dt_f;
 };

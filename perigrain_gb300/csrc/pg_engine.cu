@@ -166,7 +166,6 @@ static int mixed_setup(pg_handle* h, const pg_setup_desc* s) {
   // gather their own (padding) index for bonds they never use
   const size_t NP = (size_t)P.n_chunks * 32;
   CU(h->dalloc(&P.bref, (NP - N) * 8 + (size_t)N * 4 * D));
-  CU(h->dalloc(&P.cur_hl, (size_t)N * 2 * SF));
   CU(h->dalloc(&P.acc_f, (size_t)N * SF));
   CU(h->dalloc(&P.force_f, (size_t)N * SF));
   CU(h->dalloc(&P.extf_f, (size_t)N * SF));
@@ -177,7 +176,6 @@ static int mixed_setup(pg_handle* h, const pg_setup_desc* s) {
   P.hdt2_f = (float)P.hdt2;
   P.half_dt_f = (float)P.half_dt;
   (void)s;
-  CU(cudaMemset(P.cur_hl, 0, (size_t)N * 2 * SF * 4));
   CU(cudaMemset(P.acc_f, 0, (size_t)N * SF * 4));
   CU(cudaMemset(P.extf_f, 0, (size_t)N * SF * 4));
   CU(cudaMemset(P.force_f, 0, (size_t)N * SF * 4));
@@ -618,6 +616,15 @@ static int create_impl(const pg_setup_desc* s, const pg_config* cfg_in, pg_handl
   CU(h->dalloc(&P.clamped, N));
   CU(h->dalloc(&P.clamp_pending, N));
   CU(cudaMemcpy(P.node_grain, node_grain.data(), N * 4, cudaMemcpyHostToDevice));
+  {
+    std::vector<uint32_t> sub(N);
+    for (uint32_t i = 0; i < N; ++i) {
+      const uint32_t o = permuted ? ord.perm[i] : i;  // same grain: grain node ranges are unchanged
+      sub[i] = cfg.nl_bdry_only ? bdry_rank[i] : o - s->grain_node_offset[node_grain[i]];
+    }
+    CU(h->dalloc(&P.node_sub, N));
+    CU(cudaMemcpy(P.node_sub, sub.data(), (size_t)N * 4, cudaMemcpyHostToDevice));
+  }
   CU(cudaMemcpy(P.bdry_rank, bdry_rank.data(), N * 4, cudaMemcpyHostToDevice));
   CU(cudaMemcpy(P.clamped, clamped.data(), N, cudaMemcpyHostToDevice));
   CU(cudaMemset(P.clamp_pending, 0, N));

@@ -229,7 +229,7 @@ __global__ void __launch_bounds__(128) k_force(const Dev P) {
         grain_box<D>(P, gq, qmn, qmx);
         if (!boxes_touch<D>(bmn, bmx, qmn, qmx, in.contact_rad)) return;
       }
-      const uint32_t sub = P.nl_bdry_only ? P.bdry_rank[q] : (orig_of(P, q) - P.grain[gq].node_begin);
+      const uint32_t sub = P.node_sub[q];
       const unsigned long long key =
           ((unsigned long long)(same ? 0u : 1u) << 63) | ((unsigned long long)gq << 32) | sub;
       insert_cand<D>(keys, idx, nc, key, q, P);

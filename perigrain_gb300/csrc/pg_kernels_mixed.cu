@@ -234,27 +234,18 @@ __global__ void __launch_bounds__(256) k_predict_mx(const Dev P) {
     for (int c = 0; c < D; ++c) cu[c] = ps[c] + dp[c];
     stv<D>(P.cur, d, cu);
     const InstDev& in = P.inst[gr.inst];
-    // images relative to the fixed frame with candidate lists (independent of the grid refit of
-    // the step before), else to this step's grid origin
-    const double* org = in.rel_frame ? in.xorigin : in.origin;
-    double rel[D];
+    // the FP32 position image: offset from the fixed frame with candidate lists (independent of
+    // the grid refit of the step before), else from this step's grid origin; formed in FP32 from
+    // the truncated CurrPos (integer instructions) -- an FP64 subtraction here would run on the
+    // narrow FP64 pipe, and the image only feeds the cell keys and the FP32 prefilter
     float rf[4] = {0.f, 0.f, 0.f, 0.f};
     bool ok = true;
-    float rh[D], rl[D];
     for (int c = 0; c < D; ++c) {
       if (((__double_as_longlong(cu[c]) >> 52) & 0x7ff) == 0x7ff) ok = false;  // inf or NaN
-      rel[c] = cu[c] - org[c];
-      split_hl(rel[c], &rh[c], &rl[c]);
-      rf[c] = rh[c];
+      double cut;
+      rf[c] = trunc_f32(cu[c], &cut) - in.org_f[c];
     }
     if (!ok) set_status(P.status, PG_ENAN);
-    if constexpr (D == 2) {
-      reinterpret_cast<float4*>(P.cur_hl)[d] = make_float4(rh[0], rh[1], rl[0], rl[1]);
-    } else {
-      float4* q = reinterpret_cast<float4*>(P.cur_hl) + 2ull * d;
-      q[0] = make_float4(rh[0], rh[1], rh[2], 0.f);
-      q[1] = make_float4(rl[0], rl[1], rl[2], 0.f);
-    }
     if constexpr (D == 2) {
       reinterpret_cast<float2*>(P.curf)[d] = make_float2(rf[0], rf[1]);
     } else {
@@ -338,7 +329,15 @@ __device__ __forceinline__ void bond_term(const float (&dh)[D], const float (&dl
 // ---------------------------------------------------------------------------------------------
 // fused force + integrate, FP32 forces
 // ---------------------------------------------------------------------------------------------
-template <int D, bool REC, bool GC>
+// The input's index of device node i in a force kernel: PERM (the handle's node layout differs
+// from the input order) looks it up, otherwise the layout is the input order and i is it.
+template <bool PERM>
+__device__ __forceinline__ uint32_t input_index(const Dev& P, uint32_t i) {
+  if constexpr (PERM) return P.node_orig[i];
+  return i;
+}
+
+template <int D, bool REC, bool GC, bool PERM>
 __global__ void __launch_bounds__(128) k_force_mx(const Dev P) {
   pdl_enter();
   const uint32_t d = blockIdx.x * blockDim.x + threadIdx.x;
@@ -461,8 +460,8 @@ __global__ void __launch_bounds__(128) k_force_mx(const Dev P) {
   if ((selfc || other) && p_bdry && (!P.cand_q || ncl > 0)) {
     double bmn[D], bmx[D];
     grain_box<D>(P, g, bmn, bmx);
-    float ph[D], pl[D];
-    ld_hl<D>(P.cur_hl, d, ph, pl);
+    float ph[D];
+    ldf<D>(P.curf, d, ph);
     int32_t cc[3] = {0, 0, 0};
     for (int c = 0; c < D; ++c) cc[c] = cell_coord(ph[c] + in.frame_off_f[c], in.inv_cell_f, in.dims[c]);
     const float thr2 = in.pre_f * in.pre_f;
@@ -489,7 +488,7 @@ __global__ void __launch_bounds__(128) k_force_mx(const Dev P) {
         grain_box<D>(P, gq, qmn, qmx);
         if (!boxes_touch<D>(bmn, bmx, qmn, qmx, in.contact_rad)) return;
       }
-      const uint32_t sub = P.nl_bdry_only ? P.bdry_rank[q] : (orig_of(P, q) - P.grain[gq].node_begin);
+      const uint32_t sub = P.node_sub[q];
       const unsigned long long key =
           ((unsigned long long)(same ? 0u : 1u) << 63) | ((unsigned long long)gq << 32) | sub;
       insert_cand<D>(keys, idx, nc, key, q, P);
@@ -518,6 +517,8 @@ __global__ void __launch_bounds__(128) k_force_mx(const Dev P) {
       }
     }
     const uint32_t mydeg = P.node_deg[d];
+    // the pair log hashes input indices (the node's own looked up once; recorded runs only)
+    const unsigned long long od_hash = P.record_pairs ? ((unsigned long long)input_index<PERM>(P, d) << 32) : 0ull;
     const float Kn0 = (float)in.normal_stiffness;
     const float mu0 = (float)in.friction_coefficient, zeta0 = (float)in.damping_ratio;
     const float rho = (float)gr.rho, dtf = (float)P.dt;
@@ -565,7 +566,7 @@ __global__ void __launch_bounds__(128) k_force_mx(const Dev P) {
       for (int c = 0; c < D; ++c) dir[c] = (float)dir64[c];
       if (P.record_pairs) {
         my_pairs += 1;
-        my_hash += splitmix64(((unsigned long long)orig_of(P, d) << 32) | orig_of(P, q));
+        my_hash += splitmix64(od_hash | input_index<PERM>(P, q));
       }
       if (dn == 0.f) my_close += 1;
       const float inv = 1.f / dn;
@@ -647,7 +648,7 @@ __global__ void __launch_bounds__(128) k_force_mx(const Dev P) {
         rec.a_t1 = 0;
         rec.a_t2 = 0;
         rec.a_damp = 0;
-        rec.gid = P.nl_bdry_only ? (gr.node_begin + P.bdry_rank[d]) : orig_of(P, d);
+        rec.gid = P.nl_bdry_only ? (gr.node_begin + P.bdry_rank[d]) : input_index<PERM>(P, d);
         rec.side = (uint16_t)side;
         rec.has_fric = 0;
         rec.has_damp = 0;
@@ -765,7 +766,7 @@ __global__ void __launch_bounds__(128) k_force_mx(const Dev P) {
         }
         P.clamp_pending[d] = 1;
       }
-      if (P.worm) worm_clamp<D>(orig_of(P, d) - gr.node_begin, worm_phase(t), a, v);
+      if (P.worm) worm_clamp<D>(input_index<PERM>(P, d) - gr.node_begin, worm_phase(t), a, v);
       stvf<D>(P.acc_f, d, a);
       stv<D>(P.vel_out, d, v);
     } else {
@@ -796,6 +797,25 @@ __global__ void __launch_bounds__(128) k_force_mx(const Dev P) {
   if (my_close) atomicAdd(P.too_close, my_close);
 }
 
+// The force kernel's variants: mask recording (REC), per-grain contact parameters (GC) and a node
+// layout other than the input order (PERM) are compiled in only where used, so the plain kernel
+// keeps its register budget.
+template <int D>
+static void launch_force_mx(const Dev& P, dim3 grid, dim3 block, cudaStream_t s, bool pdl, bool rec) {
+  const bool perm = P.node_orig != nullptr;
+  if (P.grain_contact) {
+    if (rec) perm ? launch_k(k_force_mx<D, true, true, true>, grid, block, 0, s, pdl, P)
+                  : launch_k(k_force_mx<D, true, true, false>, grid, block, 0, s, pdl, P);
+    else perm ? launch_k(k_force_mx<D, false, true, true>, grid, block, 0, s, pdl, P)
+              : launch_k(k_force_mx<D, false, true, false>, grid, block, 0, s, pdl, P);
+  } else {
+    if (rec) perm ? launch_k(k_force_mx<D, true, false, true>, grid, block, 0, s, pdl, P)
+                  : launch_k(k_force_mx<D, true, false, false>, grid, block, 0, s, pdl, P);
+    else perm ? launch_k(k_force_mx<D, false, false, true>, grid, block, 0, s, pdl, P)
+              : launch_k(k_force_mx<D, false, false, false>, grid, block, 0, s, pdl, P);
+  }
+}
+
 template <int D>
 static void launch_mx(const Dev& P, const LaunchCfg& L, cudaStream_t s, uint64_t* launches, cudaEvent_t e0,
                       cudaEvent_t e1, bool rec) {
@@ -811,16 +831,8 @@ static void launch_mx(const Dev& P, const LaunchCfg& L, cudaStream_t s, uint64_t
     *launches += 1;
   }
   if (e0) cudaEventRecord(e0, s);
-  // variants: mask recording (REC) and per-grain contact parameters (GC) are compiled in only
-  // where used, so the plain kernel keeps its register budget
   const dim3 grid(cdiv(nthr, L.force_block)), block(L.force_block);
-  if (P.grain_contact) {
-    if (rec) launch_k(k_force_mx<D, true, true>, grid, block, 0, s, pdl, P);
-    else launch_k(k_force_mx<D, false, true>, grid, block, 0, s, pdl, P);
-  } else {
-    if (rec) launch_k(k_force_mx<D, true, false>, grid, block, 0, s, pdl, P);
-    else launch_k(k_force_mx<D, false, false>, grid, block, 0, s, pdl, P);
-  }
+  launch_force_mx<D>(P, grid, block, s, pdl, rec);
   if (e1) cudaEventRecord(e1, s);
   launch_k(k_finalize<D>, finalize_blocks(P.I), FINAL_THREADS, P.wrec_smem ? FINAL_SMEM : 0, s, pdl, P);
   *launches += 2;
@@ -831,12 +843,17 @@ cudaError_t kernels_mixed_init() {
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_finalize<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, FINAL_SMEM);
   if (e != cudaSuccess) return e;
   // the recording variants of the force kernel have local frames of about 1.1 KB
-  const void* fs[] = {(const void*)k_force_mx<2, false, false>, (const void*)k_force_mx<2, false, true>,
-                      (const void*)k_force_mx<2, true, false>,  (const void*)k_force_mx<2, true, true>,
-                      (const void*)k_force_mx<3, false, false>, (const void*)k_force_mx<3, false, true>,
-                      (const void*)k_force_mx<3, true, false>,  (const void*)k_force_mx<3, true, true>};
+  const void* fs[] = {
+      (const void*)k_force_mx<2, false, false, false>, (const void*)k_force_mx<2, false, true, false>,
+      (const void*)k_force_mx<2, true, false, false>,  (const void*)k_force_mx<2, true, true, false>,
+      (const void*)k_force_mx<3, false, false, false>, (const void*)k_force_mx<3, false, true, false>,
+      (const void*)k_force_mx<3, true, false, false>,  (const void*)k_force_mx<3, true, true, false>,
+      (const void*)k_force_mx<2, false, false, true>,  (const void*)k_force_mx<2, false, true, true>,
+      (const void*)k_force_mx<2, true, false, true>,   (const void*)k_force_mx<2, true, true, true>,
+      (const void*)k_force_mx<3, false, false, true>,  (const void*)k_force_mx<3, false, true, true>,
+      (const void*)k_force_mx<3, true, false, true>,   (const void*)k_force_mx<3, true, true, true>};
   size_t need = 0;
-  e = max_local_bytes(fs, 8, &need);
+  e = max_local_bytes(fs, 16, &need);
   return e == cudaSuccess ? ensure_local_bytes(need) : e;
 }
 
@@ -867,13 +884,7 @@ static void launch_mx_body(const Dev& P, const LaunchCfg& L, cudaStream_t s, boo
     *launches += 1;
   }
   const dim3 grid(cdiv(P.n_chunks * 32, L.force_block)), block(L.force_block);
-  if (P.grain_contact) {
-    if (rec) launch_k(k_force_mx<D, true, true>, grid, block, 0, s, pdl, P);
-    else launch_k(k_force_mx<D, false, true>, grid, block, 0, s, pdl, P);
-  } else {
-    if (rec) launch_k(k_force_mx<D, true, false>, grid, block, 0, s, pdl, P);
-    else launch_k(k_force_mx<D, false, false>, grid, block, 0, s, pdl, P);
-  }
+  launch_force_mx<D>(P, grid, block, s, pdl, rec);
   *launches += 1;
 }
 
