@@ -245,6 +245,10 @@ int pg_get_device_status(pg_handle* h, int32_t* status, uint64_t* too_close_even
  * has reported PG_ETIMEOUT, pg_step returns PG_ETIMEOUT without launching (create a new handle).
  * PG_EINVAL without candidate lists or cooperative launch. */
 int pg_debug_grid_barrier(pg_handle* h, uint32_t arrivals);
+/* Test hook for the FP64 path's integer division and square root: for host arrays of n doubles
+ * (0 <= n <= 2^26) computes quot[i] = a[i] / b[i] and root[i] = sqrt(|a[i]|) on the current
+ * device with the routines the FP64 force kernel uses, for comparison with IEEE results. */
+int pg_debug_ieee64(const double* a, const double* b, int64_t n, double* quot, double* root);
 /* Launch configuration in use (after autotuning): force-kernel block size, grid cells per node. */
 int pg_get_launch_config(pg_handle* h, uint32_t* block_size, uint32_t* cells_per_node);
 /* Contact candidate-list skin in use (fraction of R_c; 0: grid search every step). */

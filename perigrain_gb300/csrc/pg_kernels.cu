@@ -20,6 +20,7 @@
 
 #include "pg_common.cuh"
 #include "pg_device.cuh"
+#include "pg_ieee64.cuh"
 #include "pg_kernels.h"
 
 namespace pg {
@@ -168,10 +169,12 @@ __global__ void __launch_bounds__(128) k_force(const Dev P) {
         for (int c = 0; c < D; ++c) e[c] = (dj[c] - dp[c]) + (xj[c] - xp[c]);
         double n2 = e[0] * e[0];
         for (int c = 1; c < D; ++c) n2 = n2 + e[c] * e[c];
-        const double en = sqrt(n2);
-        const double str = (en - xin) / xin;
+        // sqrt and the divisions on the integer pipe, bit-identical to the IEEE operations
+        const double en = ieee64::sqrt_rn(n2);
+        const double str = ieee64::div_rn(en - xin, xin);
         const double sc = (gr.cnot * str) * P.vol[j];
-        for (int c = 0; c < D; ++c) f[c] = f[c] + sc * (e[c] / en);
+        const ieee64::Divisor den = ieee64::make_divisor(en);
+        for (int c = 0; c < D; ++c) f[c] = f[c] + sc * ieee64::div_rn(e[c], den);
         if (brk && str > gr.snot) {
           bit = false;
           P.break_step[s] = t;
@@ -261,7 +264,7 @@ __global__ void __launch_bounds__(128) k_force(const Dev P) {
       for (int c = 0; c < D; ++c) dir[c] = xq[c] - xpc[c];
       double n2 = dir[0] * dir[0];
       for (int c = 1; c < D; ++c) n2 = n2 + dir[c] * dir[c];
-      const double dn = sqrt(n2);
+      const double dn = ieee64::sqrt_rn(n2);
       double Rc = in.contact_rad, Kn = in.normal_stiffness;
       double zeta = in.damping_ratio, mu = in.friction_coefficient;
       if constexpr (GC) {
@@ -282,14 +285,9 @@ __global__ void __launch_bounds__(128) k_force(const Dev P) {
         for (int c = 0; c < D; ++c) r[c] = pp[c] - pq[c];
         double r2 = r[0] * r[0];
         for (int c = 1; c < D; ++c) r2 = r2 + r[c] * r[c];
-        const double ref = sqrt(r2);
-        if (ref < in.contact_rad) {
-          Rc = ref;
-          Kn = gr.cnot / ref;
-        } else {
-          Rc = in.contact_rad;
-          Kn = gr.cnot / in.contact_rad;
-        }
+        const double ref = ieee64::sqrt_rn(r2);
+        Rc = ref < in.contact_rad ? ref : in.contact_rad;
+        Kn = ieee64::div_rn(gr.cnot, Rc);
       }
       if (!(dn <= Rc)) continue;
       if (P.record_pairs) {
@@ -298,7 +296,10 @@ __global__ void __launch_bounds__(128) k_force(const Dev P) {
       }
       if (dn == 0.0) my_close += 1;
       double u[D];
-      for (int c = 0; c < D; ++c) u[c] = dir[c] / dn;
+      {
+        const ieee64::Divisor ddn = ieee64::make_divisor(dn);
+        for (int c = 0; c < D; ++c) u[c] = ieee64::div_rn(dir[c], ddn);
+      }
       const double crc = Rc - dn;
       const double nvol = P.vol[q];
       const double s1 = ((-Kn) * crc) * nvol;
@@ -306,7 +307,7 @@ __global__ void __launch_bounds__(128) k_force(const Dev P) {
       for (int c = 0; c < D; ++c) fc[c] = s1 * u[c];
       double cf2 = fc[0] * fc[0];
       for (int c = 1; c < D; ++c) cf2 = cf2 + fc[c] * fc[c];
-      const double cfn = sqrt(cf2);
+      const double cfn = ieee64::sqrt_rn(cf2);
       for (int c = 0; c < D; ++c) f[c] = f[c] + fc[c];
       uint32_t fr = 0;
       if (P.allow_damping || P.allow_friction) {
@@ -316,7 +317,7 @@ __global__ void __launch_bounds__(128) k_force(const Dev P) {
         double rvp = rv[0] * u[0];
         for (int c = 1; c < D; ++c) rvp = rvp + rv[c] * u[c];
         if (P.allow_damping) {
-          const double dc = ((2.0 * zeta) * sqrt(Kn * gr.rho)) * sqrt(nvol);
+          const double dc = ((2.0 * zeta) * ieee64::sqrt_rn(Kn * gr.rho)) * ieee64::sqrt_rn(nvol);
           for (int c = 0; c < D; ++c) f[c] = f[c] + ((-dc) * (rvp * u[c]));
         }
         if (P.allow_friction) {
@@ -324,15 +325,16 @@ __global__ void __launch_bounds__(128) k_force(const Dev P) {
           for (int c = 0; c < D; ++c) tg[c] = rv[c] - (rvp * u[c]);
           double t2 = tg[0] * tg[0];
           for (int c = 1; c < D; ++c) t2 = t2 + tg[c] * tg[c];
-          const double tn = sqrt(t2);
+          const double tn = ieee64::sqrt_rn(t2);
           if (tn > 0) {
             double sfr = (-mu) * cfn;
             fr = (D == 2 && (tg[1] * u[0] - tg[0] * u[1]) < 0) ? FR_SLIDE_NEG : FR_SLIDE;
-            if (tn < (((mu * cfn) * P.dt) / gr.rho)) {
-              sfr = ((-tn) / gr.rho) / P.dt;
+            if (tn < ieee64::div_rn((mu * cfn) * P.dt, gr.rho)) {
+              sfr = ieee64::div_rn(ieee64::div_rn(-tn, gr.rho), P.dt);
               fr = FR_STICK;
             }
-            for (int c = 0; c < D; ++c) f[c] = f[c] + sfr * (tg[c] / tn);
+            const ieee64::Divisor dtn = ieee64::make_divisor(tn);
+            for (int c = 0; c < D; ++c) f[c] = f[c] + sfr * ieee64::div_rn(tg[c], dtn);
           }
         }
       }
@@ -606,6 +608,25 @@ uint32_t grid_coop_blocks(const Dev& P, int device) {
 
 const void* force_kernel_ptr(uint32_t dim) {
   return dim == 2 ? (const void*)k_force<2, false, false> : (const void*)k_force<3, false, false>;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Check kernel of the integer FP64 division and square root: quot[i] = a[i] / b[i] and
+// root[i] = sqrt(|a[i]|) through pg_ieee64.cuh, both through a prepared divisor and directly.
+// ---------------------------------------------------------------------------------------------
+__global__ void k_ieee64_check(const double* a, const double* b, int64_t n, double* quot, double* root) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  quot[i] = ieee64::div_rn(a[i], ieee64::make_divisor(b[i]));
+  root[i] = ieee64::sqrt_rn(fabs(a[i]));
+}
+
+cudaError_t launch_ieee64_check(const double* a, const double* b, int64_t n, double* quot, double* root,
+                                cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  const int64_t blocks = (n + 255) / 256;
+  k_ieee64_check<<<(unsigned)blocks, 256, 0, s>>>(a, b, n, quot, root);
+  return cudaGetLastError();
 }
 
 }  // namespace pg
