@@ -245,10 +245,14 @@ int pg_get_device_status(pg_handle* h, int32_t* status, uint64_t* too_close_even
  * has reported PG_ETIMEOUT, pg_step returns PG_ETIMEOUT without launching (create a new handle).
  * PG_EINVAL without candidate lists or cooperative launch. */
 int pg_debug_grid_barrier(pg_handle* h, uint32_t arrivals);
-/* Test hook for the FP64 path's integer division and square root: for host arrays of n doubles
- * (0 <= n <= 2^26) computes quot[i] = a[i] / b[i] and root[i] = sqrt(|a[i]|) on the current
- * device with the routines the FP64 force kernel uses, for comparison with IEEE results. */
-int pg_debug_ieee64(const double* a, const double* b, int64_t n, double* quot, double* root);
+/* Test hook for the FP64 path's integer arithmetic (correctly rounded division, square root,
+ * addition, subtraction, multiplication and FP32 -> FP64 conversion on the integer pipe): for host
+ * arrays of n doubles (0 <= n <= 2^26) computes out[i] = a[i] / b[i] (op PG_IEEE_DIV),
+ * sqrt(|a[i]|) (PG_IEEE_SQRT), a[i] + b[i] (PG_IEEE_ADD), a[i] - b[i] (PG_IEEE_SUB), a[i] * b[i]
+ * (PG_IEEE_MUL) or (double)(float)a[i] (PG_IEEE_WIDEN) on the current device with the routines
+ * the kernels use, for comparison with IEEE results. PG_EINVAL for another op. */
+enum pg_ieee_op { PG_IEEE_DIV = 0, PG_IEEE_SQRT = 1, PG_IEEE_ADD = 2, PG_IEEE_SUB = 3, PG_IEEE_MUL = 4, PG_IEEE_WIDEN = 5 };
+int pg_debug_ieee64(int32_t op, const double* a, const double* b, int64_t n, double* out);
 /* Launch configuration in use (after autotuning): force-kernel block size, grid cells per node. */
 int pg_get_launch_config(pg_handle* h, uint32_t* block_size, uint32_t* cells_per_node);
 /* Contact candidate-list skin in use (fraction of R_c; 0: grid search every step). */

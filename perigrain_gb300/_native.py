@@ -122,7 +122,7 @@ PROTOTYPES = [
     ("pg_get_pair_log", C.c_int, [C.c_void_p, C.c_uint32, u64p, u64p]),
     ("pg_get_device_status", C.c_int, [C.c_void_p, i32p, u64p]),
     ("pg_debug_grid_barrier", C.c_int, [C.c_void_p, C.c_uint32]),
-    ("pg_debug_ieee64", C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
+    ("pg_debug_ieee64", C.c_int, [C.c_int32, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
     ("pg_get_launch_count", C.c_int, [C.c_void_p, u64p]),
     ("pg_get_launch_config", C.c_int, [C.c_void_p, u32p, u32p]),
     ("pg_get_contact_skin", C.c_int, [C.c_void_p, f64p]),

@@ -1251,19 +1251,19 @@ int pg_debug_grid_barrier(pg_handle* h, uint32_t arrivals) {
   return PG_OK;
 }
 
-int pg_debug_ieee64(const double* a, const double* b, int64_t n, double* quot, double* root) {
+int pg_debug_ieee64(int32_t op, const double* a, const double* b, int64_t n, double* out) {
+  if (op < PG_IEEE_DIV || op > PG_IEEE_WIDEN) return fail(PG_EINVAL, "unknown op");
   if (n < 0 || n > ((int64_t)1 << 26)) return fail(PG_EINVAL, "n out of range [0, 2^26]");
-  if (n > 0 && (!a || !b || !quot || !root)) return fail(PG_EINVAL, "null array");
+  if (n > 0 && (!a || !b || !out)) return fail(PG_EINVAL, "null array");
   if (n == 0) return PG_OK;
   const size_t bytes = (size_t)n * sizeof(double);
   double* buf = nullptr;
-  CU(cudaMalloc(&buf, 4 * bytes));
-  double *da = buf, *db = buf + n, *dq = buf + 2 * n, *dr = buf + 3 * n;
+  CU(cudaMalloc(&buf, 3 * bytes));
+  double *da = buf, *db = buf + n, *dout = buf + 2 * n;
   cudaError_t e = cudaMemcpy(da, a, bytes, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(db, b, bytes, cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = pg::launch_ieee64_check(da, db, n, dq, dr, 0);
-  if (e == cudaSuccess) e = cudaMemcpy(quot, dq, bytes, cudaMemcpyDeviceToHost);
-  if (e == cudaSuccess) e = cudaMemcpy(root, dr, bytes, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = pg::launch_ieee64_check(op, da, db, n, dout, 0);
+  if (e == cudaSuccess) e = cudaMemcpy(out, dout, bytes, cudaMemcpyDeviceToHost);
   const cudaError_t ef = cudaFree(buf);
   if (e == cudaSuccess) e = ef;
   if (e != cudaSuccess) return fail(PG_ECUDA, std::string("pg_debug_ieee64: ") + cudaGetErrorString(e));

@@ -3,9 +3,10 @@
 // GB300 executes FP64 arithmetic at about 1/64 of its FP32 rate, and an IEEE FP64 division or
 // square root expands to about ten FP64 instructions, while the integer and FP32 pipes are some
 // thirty to sixty times wider. These routines return exactly the IEEE round-to-nearest-even result,
-// the bits of `a / b` and `sqrt(x)`, whenever operands and result are normal numbers; every other
-// case (zero, subnormal, infinite or NaN operands, a result outside the normal range) is passed to
-// the FP64 hardware operation, so the functions are drop-in replacements bit for bit.
+// the bits of `a / b` and `sqrt(x)`, whenever operands and result are normal numbers, and for a
+// zero dividend over a normal divisor; every other case (zero divisor or radicand, subnormal,
+// infinite or NaN operands, a result outside the normal range) is passed to the FP64 hardware
+// operation, so the functions are drop-in replacements bit for bit.
 //
 // Division (schoolbook long division with a reciprocal estimate, Knuth TAOCP vol. 2 section 4.3.1,
 // in the form of division by a precomputed reciprocal of Granlund and Montgomery 1994). With
@@ -28,6 +29,13 @@
 // quotient taken in FP32; one more Newton step S += (M - S^2) / (2S) from the exact remainder
 // (below 2^59 in magnitude while S is within eight units) and one +-1 correction make
 // 0 <= M - S^2 <= 2S, and the remainder gives the sticky bit as for the quotient.
+//
+// Addition, subtraction and multiplication (add_rn, sub_rn, mul_rn) and the FP32 -> FP64
+// conversion (widen_f32) are provided the same way. Measured in the FP64 force kernel's bond loop
+// (bond vector e = (dj - dp) + (xj - xp)) and in the mixed path's position update, the integer
+// sum was slower than the FP64 instruction it replaced (about 40 integer instructions against one
+// FP64 add), so the kernels use only the division and square root; the others are kept, with
+// their checks, for loops where the FP64 pipe is busier.
 //
 // Host and device share the code, so the routines are tested bit for bit against the host's
 // IEEE operations as well as against the GPU's.
@@ -104,6 +112,22 @@ PG_HD float rsqrt_est(float x) {
   return (1.0f / std::sqrt(x)) * PG_IEEE64_EST_SCALE;
 #endif
 }
+// High 64 bits of a 64 x 64 bit product.
+PG_HD uint64_t umulhi64(uint64_t a, uint64_t b) {
+#ifdef __CUDA_ARCH__
+  return __umul64hi(a, b);
+#else
+  return (uint64_t)(((unsigned __int128)a * b) >> 64);
+#endif
+}
+// Leading zeros of a nonzero 64-bit word.
+PG_HD int32_t clz64(uint64_t x) {
+#ifdef __CUDA_ARCH__
+  return __clzll((long long)x);
+#else
+  return __builtin_clzll(x);
+#endif
+}
 // FP32 to int32, rounded to nearest.
 PG_HD int32_t f2i_rn(float x) {
 #ifdef __CUDA_ARCH__
@@ -113,6 +137,9 @@ PG_HD int32_t f2i_rn(float x) {
 #endif
 }
 PG_HD double hw_div(double a, double b) { return a / b; }
+PG_HD double hw_add(double a, double b) { return a + b; }
+PG_HD double hw_sub(double a, double b) { return a - b; }
+PG_HD double hw_mul(double a, double b) { return a * b; }
 PG_HD double hw_sqrt(double x) {
 #ifdef __CUDA_ARCH__
   return ::sqrt(x);
@@ -161,7 +188,11 @@ PG_HD double div_rn(double a, const Divisor& d) {
   const uint64_t ma = (ab & kFrac) | kHidden;
   const int32_t lt = ma < d.m ? 1 : 0;  // significand quotient below 1: develop one more bit
   const int32_t be = ea - d.e + 1023 - lt;
-  if (ea == 0 || ea == 0x7ff || d.e == 0 || be < 1 || be > 2045) return hw_div(a, d.b);
+  if (ea == 0 || ea == 0x7ff || d.e == 0 || be < 1 || be > 2045) {
+    // a zero over a normal divisor is a zero with the product of the signs
+    if ((ab << 1) == 0 && d.e != 0) return from_bits((ab ^ d.s) & kSign);
+    return hw_div(a, d.b);
+  }
   const uint64_t mb = d.m;
   const int32_t s3 = 13 + lt;  // k - 40
   // digit 1: q ~ ma / mb 2^20
@@ -241,6 +272,113 @@ PG_HD double sqrt_rn(double x) {
   uint64_t Mt = S >> 1;
   Mt += (S & 1ull) & ((R != 0 ? 1ull : 0ull) | (Mt & 1ull));
   return from_bits(((uint64_t)be << 52) + Mt - kHidden);
+}
+
+// Core of the IEEE round-to-nearest-even sum of two doubles given by their bits (b's sign already
+// flipped for a difference); `ok` is cleared, and the result is to be taken from the hardware,
+// unless both operands are normal and so is the result, or b is a zero and a is normal.
+// Method: the operand of larger magnitude keeps its exponent, the other significand is shifted
+// right with the shifted-out bits jammed into its lowest bit (a sticky bit nine places below the
+// guard bit), the significands are added or subtracted in 64-bit integers with the leading bit at
+// bit 62, the sum is renormalised, and bits 9..0 round it to 53 bits (Goldberg, "What every
+// computer scientist should know about floating-point arithmetic", 1991, section 1.4 on guard
+// digits).
+PG_HD uint64_t add_bits(uint64_t ab, uint64_t bb, bool* ok) {
+  const uint64_t aa = ab & ~kSign, ba = bb & ~kSign;
+  const bool sw = aa < ba;
+  const uint64_t hb = sw ? bb : ab, lb = sw ? ab : bb;  // |h| >= |l|
+  const uint64_t ha = sw ? ba : aa, la = sw ? aa : ba;
+  const int32_t eh = (int32_t)(ha >> 52), el = (int32_t)(la >> 52);
+  if (eh == 0x7ff || eh == 0 || el == 0) {
+    *ok = la == 0 && eh != 0 && eh != 0x7ff;  // normal + zero is the normal operand
+    return hb;
+  }
+  const uint64_t mh = ((ha & kFrac) | kHidden) << 10;
+  const uint64_t ml = ((la & kFrac) | kHidden) << 10;
+  const int32_t sh = eh - el;
+  uint64_t mls = 1;  // only the sticky bit remains of a significand shifted by 64 or more
+  if (sh < 64) {
+    mls = ml >> sh;
+    mls |= (mls << sh) != ml ? 1ull : 0ull;
+  }
+  int32_t e = eh;
+  uint64_t m;
+  if (((hb ^ lb) >> 63) == 0) {
+    m = mh + mls;  // below 2^64
+    if (m >> 63) {
+      m = (m >> 1) | (m & 1ull);
+      e += 1;
+    }
+  } else {
+    m = mh - mls;
+    if (m == 0) {
+      *ok = true;
+      return 0ull;  // an exact zero difference is +0 under round-to-nearest
+    }
+    const int32_t lz = clz64(m) - 1;
+    m <<= lz;
+    e -= lz;
+  }
+  *ok = e >= 1 && e <= 2045;
+  const uint64_t r = m & 0x3ffull;
+  uint64_t q = m >> 10;
+  q += (r > 0x200ull ? 1ull : 0ull) | ((r == 0x200ull ? 1ull : 0ull) & q);
+  return (hb & kSign) | (((uint64_t)e << 52) + q - kHidden);
+}
+
+// IEEE round-to-nearest-even a + b and a - b.
+PG_HD double add_rn(double a, double b) {
+  bool ok;
+  const uint64_t r = add_bits(bits(a), bits(b), &ok);
+  return ok ? from_bits(r) : hw_add(a, b);
+}
+PG_HD double sub_rn(double a, double b) {
+  bool ok;
+  const uint64_t r = add_bits(bits(a), bits(b) ^ kSign, &ok);
+  return ok ? from_bits(r) : hw_sub(a, b);
+}
+
+// IEEE round-to-nearest-even a * b: the 106-bit product of the significands from a 64 x 64 bit
+// multiplication, its top 53 bits rounded with the next bit and the rest as the sticky bit. A
+// zero times a finite number is the signed zero; other zero, subnormal, infinite or NaN operands
+// and results outside the normal range take the hardware operation.
+PG_HD double mul_rn(double a, double b) {
+  const uint64_t ab = bits(a), bb = bits(b);
+  const int32_t ea = (int32_t)((ab >> 52) & 0x7ff), eb = (int32_t)((bb >> 52) & 0x7ff);
+  const uint64_t sign = (ab ^ bb) & kSign;
+  const uint64_t ma = (ab & kFrac) | kHidden, mb = (bb & kFrac) | kHidden;
+  const uint64_t lo = ma * mb, hi = umulhi64(ma, mb);  // product in [2^104, 2^106)
+  const int32_t top = (int32_t)(hi >> 41);               // 1 when the product is >= 2^105
+  const int32_t e = ea + eb - 1023 + top;
+  if (ea == 0 || ea == 0x7ff || eb == 0 || eb == 0x7ff || e < 1 || e > 2045) {
+    if ((((ab << 1) == 0) && eb != 0x7ff) || (((bb << 1) == 0) && ea != 0x7ff)) return from_bits(sign);
+    return hw_mul(a, b);
+  }
+  const int32_t sh = 52 + top;
+  uint64_t q = (hi << (64 - sh)) | (lo >> sh);
+  const uint64_t g = (lo >> (sh - 1)) & 1ull;
+  const uint64_t st = (lo & ((1ull << (sh - 1)) - 1ull)) != 0 ? 1ull : 0ull;
+  q += g & (st | (q & 1ull));
+  return from_bits(sign | (((uint64_t)e << 52) + q - kHidden));
+}
+
+// Exact FP32 -> FP64 conversion from the bits; subnormal, infinite and NaN inputs take the
+// hardware conversion.
+PG_HD double widen_f32(float x) {
+#ifdef __CUDA_ARCH__
+  uint32_t u;
+  asm("mov.b32 %0, %1;" : "=r"(u) : "f"(x));
+#else
+  uint32_t u;
+  std::memcpy(&u, &x, 4);
+#endif
+  const uint32_t ef = (u >> 23) & 0xffu;
+  const uint64_t sign = (uint64_t)(u & 0x80000000u) << 32;
+  if (ef == 0 || ef == 0xff) {
+    if ((u << 1) == 0) return from_bits(sign);
+    return (double)x;
+  }
+  return from_bits(sign | ((uint64_t)(ef + 896u) << 52) | ((uint64_t)(u & 0x7fffffu) << 29));
 }
 
 }  // namespace ieee64

@@ -173,8 +173,13 @@ __global__ void __launch_bounds__(128) k_force(const Dev P) {
         const double en = ieee64::sqrt_rn(n2);
         const double str = ieee64::div_rn(en - xin, xin);
         const double sc = (gr.cnot * str) * P.vol[j];
-        const ieee64::Divisor den = ieee64::make_divisor(en);
-        for (int c = 0; c < D; ++c) f[c] = f[c] + sc * ieee64::div_rn(e[c], den);
+        // an unstretched bond (sc = +-0 with 0 < en < inf, so |e[c] / en| <= 1) adds +-0, which
+        // leaves f's bits unchanged (f starts at +0 and never becomes -0 under round-to-nearest)
+        const uint64_t enb = ieee64::bits(en);
+        if ((ieee64::bits(sc) << 1) != 0 || enb - 1 >= 0x7fefffffffffffffull) {
+          const ieee64::Divisor den = ieee64::make_divisor(en);
+          for (int c = 0; c < D; ++c) f[c] = f[c] + sc * ieee64::div_rn(e[c], den);
+        }
         if (brk && str > gr.snot) {
           bit = false;
           P.break_step[s] = t;
@@ -611,21 +616,30 @@ const void* force_kernel_ptr(uint32_t dim) {
 }
 
 // ---------------------------------------------------------------------------------------------
-// Check kernel of the integer FP64 division and square root: quot[i] = a[i] / b[i] and
-// root[i] = sqrt(|a[i]|) through pg_ieee64.cuh, both through a prepared divisor and directly.
+// Check kernel of the integer FP64 arithmetic (pg_ieee64.cuh): out[i] = op(a[i], b[i]), the
+// division through a prepared divisor.
 // ---------------------------------------------------------------------------------------------
-__global__ void k_ieee64_check(const double* a, const double* b, int64_t n, double* quot, double* root) {
+__global__ void k_ieee64_check(int32_t op, const double* a, const double* b, int64_t n, double* out) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  quot[i] = ieee64::div_rn(a[i], ieee64::make_divisor(b[i]));
-  root[i] = ieee64::sqrt_rn(fabs(a[i]));
+  const double x = a[i], y = b[i];
+  double r;
+  switch (op) {
+    case PG_IEEE_DIV: r = ieee64::div_rn(x, ieee64::make_divisor(y)); break;
+    case PG_IEEE_SQRT: r = ieee64::sqrt_rn(fabs(x)); break;
+    case PG_IEEE_ADD: r = ieee64::add_rn(x, y); break;
+    case PG_IEEE_SUB: r = ieee64::sub_rn(x, y); break;
+    case PG_IEEE_MUL: r = ieee64::mul_rn(x, y); break;
+    default: r = ieee64::widen_f32((float)x); break;
+  }
+  out[i] = r;
 }
 
-cudaError_t launch_ieee64_check(const double* a, const double* b, int64_t n, double* quot, double* root,
+cudaError_t launch_ieee64_check(int32_t op, const double* a, const double* b, int64_t n, double* out,
                                 cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
   const int64_t blocks = (n + 255) / 256;
-  k_ieee64_check<<<(unsigned)blocks, 256, 0, s>>>(a, b, n, quot, root);
+  k_ieee64_check<<<(unsigned)blocks, 256, 0, s>>>(op, a, b, n, out);
   return cudaGetLastError();
 }
 

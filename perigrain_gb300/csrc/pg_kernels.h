@@ -45,9 +45,9 @@ const void* force_kernel_ptr(uint32_t dim);
 // Blocks of the cooperative grid build (k_grid_coop): every block resident at once (occupancy x
 // SMs), no more than the work needs; 0 when the device has no cooperative launch.
 uint32_t grid_coop_blocks(const Dev& P, int device);
-// quot[i] = a[i] / b[i] and root[i] = sqrt(|a[i]|) through the integer FP64 routines
-// (pg_ieee64.cuh); device pointers, n < 2^31 * 256.
-cudaError_t launch_ieee64_check(const double* a, const double* b, int64_t n, double* quot, double* root,
+// out[i] = op(a[i], b[i]) through the integer FP64 routines (pg_ieee64.cuh), op a pg_ieee_op;
+// device pointers, n < 2^31 * 256.
+cudaError_t launch_ieee64_check(int32_t op, const double* a, const double* b, int64_t n, double* out,
                                 cudaStream_t s);
 
 }  // namespace pg
