@@ -28,6 +28,7 @@
 
 #include "../../include/perigrain.h"
 #include "pg_bonds.h"
+#include "pg_ieee64.cuh"
 
 namespace pg {
 
@@ -227,7 +228,7 @@ __device__ __forceinline__ double mm_value(const MaxiMin& M, double x, double y)
   double m = INFINITY;
   for (int k = 0; k < M.nc; ++k) {
     const double cx = M.at(R_CX, k), cy = M.at(R_CY, k);
-    m = fmin(m, sqrt((x - cx) * (x - cx) + (y - cy) * (y - cy)) - M.at(R_CR, k));
+    m = fmin(m, ieee64::sqrt_rn((x - cx) * (x - cx) + (y - cy) * (y - cy)) - M.at(R_CR, k));
   }
   for (int l = 0; l < M.nl; ++l) m = fmin(m, fabs(M.at(R_AX, l) * x + M.at(R_AY, l) * y + M.at(R_AB, l)));
   return m;
@@ -251,7 +252,7 @@ __device__ __forceinline__ void min_norm(const MaxiMin& M, int n, double* ox, do
       const double dx = M.at(R_GX, j) - gix, dy = M.at(R_GY, j) - giy;
       const double dd = dx * dx + dy * dy;
       if (dd <= 0.0) continue;
-      const double t = clampd(-(gix * dx + giy * dy) / dd, 0.0, 1.0);
+      const double t = clampd(ieee64::div_rn(-(gix * dx + giy * dy), dd), 0.0, 1.0);
       const double px = gix + t * dx, py = giy + t * dy;
       const double p2 = px * px + py * py;
       if (p2 < bn) {
@@ -287,10 +288,11 @@ __device__ __forceinline__ double mm_ascent(const MaxiMin& M, double* px, double
     int n = 0;
     for (int k = 0; k < M.nc; ++k) {
       const double dx = x - M.at(R_CX, k), dy = y - M.at(R_CY, k);
-      const double d = sqrt(dx * dx + dy * dy);
+      const double d = ieee64::sqrt_rn(dx * dx + dy * dy);
       if (d - M.at(R_CR, k) <= fx + step && d > 0.0) {
-        M.at(R_GX, n) = dx / d;
-        M.at(R_GY, n) = dy / d;
+        const ieee64::Divisor dd = ieee64::make_divisor(d);
+        M.at(R_GX, n) = ieee64::div_rn(dx, dd);
+        M.at(R_GY, n) = ieee64::div_rn(dy, dd);
         ++n;
       }
     }
@@ -308,12 +310,12 @@ __device__ __forceinline__ double mm_ascent(const MaxiMin& M, double* px, double
     // box faces: no motion through a face the point sits on
     if ((x <= M.lo[0] && dx < 0.0) || (x >= M.hi[0] && dx > 0.0)) dx = 0.0;
     if ((y <= M.lo[1] && dy < 0.0) || (y >= M.hi[1] && dy > 0.0)) dy = 0.0;
-    const double nd = sqrt(dx * dx + dy * dy);
+    const double nd = ieee64::sqrt_rn(dx * dx + dy * dy);
     if (nd < 1e-12) {
       step *= 0.5;
       continue;
     }
-    const double s = 0.5 * step / nd;
+    const double s = ieee64::div_rn(0.5 * step, nd);
     const double nx = clampd(x + s * dx, M.lo[0], M.hi[0]), ny = clampd(y + s * dy, M.lo[1], M.hi[1]);
     const double fn = mm_value(M, nx, ny);
     if (fn > fx) {
