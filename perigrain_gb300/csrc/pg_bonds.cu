@@ -15,6 +15,7 @@
 
 #include "../../include/perigrain.h"
 #include "pg_bonds.h"
+#include "pg_bond_threshold.h"
 #include "pg_device.cuh"
 
 namespace pg {
@@ -163,9 +164,10 @@ __global__ void kb_scatter(uint32_t n, BondScratch S) {
   if (i < n) S.sorted[S.cell_start[S.key[i]] + S.rank[i]] = i;
 }
 
-// Visit every partner j > i of node i within delta, in the grid's cell order: f(j).
+// Visit every partner j > i of node i within delta, in the grid's cell order: f(j). The test
+// sqrt(s) <= delta is made as s <= s_max, s_max = bond_s_max(delta): the same outcome for every s.
 template <class F>
-__device__ __forceinline__ void for_partners(const double* pos, uint32_t i, uint32_t dim, double delta,
+__device__ __forceinline__ void for_partners(const double* pos, uint32_t i, uint32_t dim, double s_max,
                                              const BondGrid& g, const BondScratch& S, F f) {
   int32_t cc[3];
   const double* pi = pos + (size_t)i * dim;
@@ -183,7 +185,7 @@ __device__ __forceinline__ void for_partners(const double* pos, uint32_t i, uint
         const double* pj = pos + (size_t)j * dim;
         double s = (pj[0] - pi[0]) * (pj[0] - pi[0]);
         for (uint32_t c = 1; c < dim; ++c) s = s + (pj[c] - pi[c]) * (pj[c] - pi[c]);
-        if (!(sqrt(s) <= delta)) continue;
+        if (!(s <= s_max)) continue;
         f(j);
       }
     }
@@ -193,13 +195,13 @@ __device__ __forceinline__ void for_partners(const double* pos, uint32_t i, uint
 // ascending) at its offset: the partners go to the row in visit order and are sorted there; a row
 // that crosses `capacity` gets its smallest partners that fit, picked one at a time.
 template <bool WRITE>
-__global__ void kb_pairs(const double* pos, uint32_t n, uint32_t dim, double delta, BondGrid g, BondScratch S,
+__global__ void kb_pairs(const double* pos, uint32_t n, uint32_t dim, double s_max, BondGrid g, BondScratch S,
                          uint32_t* pairs, uint64_t capacity) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   if (!WRITE) {
     uint32_t cnt = 0;
-    for_partners(pos, i, dim, delta, g, S, [&](uint32_t) { ++cnt; });
+    for_partners(pos, i, dim, s_max, g, S, [&](uint32_t) { ++cnt; });
     S.pcount[i] = cnt;
     if (cnt > (uint32_t)MAX_PARTNERS) atomicCAS(S.error, 0, (int32_t)PG_ECAPACITY);
     return;
@@ -209,7 +211,7 @@ __global__ void kb_pairs(const double* pos, uint32_t n, uint32_t dim, double del
   if (cnt == 0 || off >= capacity) return;
   if (off + cnt <= capacity) {
     uint32_t k = 0;
-    for_partners(pos, i, dim, delta, g, S, [&](uint32_t j) {
+    for_partners(pos, i, dim, s_max, g, S, [&](uint32_t j) {
       if (k < cnt) pairs[2 * (off + k) + 1] = j;
       ++k;
     });
@@ -228,7 +230,7 @@ __global__ void kb_pairs(const double* pos, uint32_t n, uint32_t dim, double del
     uint32_t prev = i;
     for (uint64_t k = off; k < capacity; ++k) {
       uint32_t best = 0xffffffffu;
-      for_partners(pos, i, dim, delta, g, S, [&](uint32_t j) {
+      for_partners(pos, i, dim, s_max, g, S, [&](uint32_t j) {
         if (j > prev && j < best) best = j;
       });
       pairs[2 * k] = i;
@@ -290,6 +292,7 @@ int run_bond_build(const double* pos, uint32_t n, uint32_t dim, double delta, ui
     ext = std::fmax(ext, hi[c] - lo[c]);
   }
   double cell = delta > 0 ? delta * (1 + 1e-6) : std::fmax(ext, 1e-300) / 64;
+  const double s_max = bond_s_max(delta);
   for (int it = 0; it < 200; ++it) {
     uint64_t cells = 1;
     for (uint32_t c = 0; c < dim; ++c) cells *= (uint64_t)((hi[c] - lo[c]) / cell) + 1;
@@ -323,12 +326,12 @@ int run_bond_build(const double* pos, uint32_t n, uint32_t dim, double delta, ui
   }
   // 4. count partners, row offsets, write rows
   if (e == cudaSuccess) {
-    kb_pairs<false><<<cdivb(n, BT), BT, 0, st>>>(pos, n, dim, delta, g, S, pairs, capacity);
+    kb_pairs<false><<<cdivb(n, BT), BT, 0, st>>>(pos, n, dim, s_max, g, S, pairs, capacity);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = scan_u32(S.pcount, n, S.poff, S, st);
   if (e == cudaSuccess) {
-    kb_pairs<true><<<cdivb(n, 128), 128, 0, st>>>(pos, n, dim, delta, g, S, pairs, capacity);
+    kb_pairs<true><<<cdivb(n, 128), 128, 0, st>>>(pos, n, dim, s_max, g, S, pairs, capacity);
     e = cudaGetLastError();
   }
   uint32_t total = 0;
