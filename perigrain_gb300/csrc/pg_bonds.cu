@@ -15,7 +15,7 @@
 
 #include "../../include/perigrain.h"
 #include "pg_bonds.h"
-#include "pg_bond_threshold.h"
+#include "pg_sqrt_threshold.h"
 #include "pg_device.cuh"
 
 namespace pg {
@@ -165,7 +165,7 @@ __global__ void kb_scatter(uint32_t n, BondScratch S) {
 }
 
 // Visit every partner j > i of node i within delta, in the grid's cell order: f(j). The test
-// sqrt(s) <= delta is made as s <= s_max, s_max = bond_s_max(delta): the same outcome for every s.
+// sqrt(s) <= delta is made as s <= s_max, s_max = sqrt_le_max(delta): the same outcome for every s.
 template <class F>
 __device__ __forceinline__ void for_partners(const double* pos, uint32_t i, uint32_t dim, double s_max,
                                              const BondGrid& g, const BondScratch& S, F f) {
@@ -292,7 +292,7 @@ int run_bond_build(const double* pos, uint32_t n, uint32_t dim, double delta, ui
     ext = std::fmax(ext, hi[c] - lo[c]);
   }
   double cell = delta > 0 ? delta * (1 + 1e-6) : std::fmax(ext, 1e-300) / 64;
-  const double s_max = bond_s_max(delta);
+  const double s_max = sqrt_le_max(delta);
   for (int it = 0; it < 200; ++it) {
     uint64_t cells = 1;
     for (uint32_t c = 0; c < dim; ++c) cells *= (uint64_t)((hi[c] - lo[c]) / cell) + 1;

@@ -69,6 +69,7 @@ inline void set_grain_f(GrainDev& g) {
 
 struct InstDev {
   double contact_rad, normal_stiffness, friction_coefficient, damping_ratio;
+  double contact_s_max;  // sqrt_le_max(contact_rad): a squared distance above it rules contact out
   double origin[3];     // lower corner of this step's grid
   double xorigin[3];    // fixed origin of the FP32 hi/lo bond reference positions (mixed path)
   double cell;          // grid cell edge (>= 1.0625 contact_rad)

@@ -16,6 +16,7 @@
 #include "pg_device.cuh"
 #include "pg_handle.h"
 #include "pg_order.h"
+#include "pg_sqrt_threshold.h"
 #include "pg_kernels.h"
 #include "pg_kernels_mixed.h"
 
@@ -754,6 +755,7 @@ static int create_impl(const pg_setup_desc* s, const pg_config* cfg_in, pg_handl
     InstDev& in = h->inst_host[k];
     std::memset(&in, 0, sizeof(in));
     in.contact_rad = s->contact_radius[k];
+    in.contact_s_max = pg::sqrt_le_max(in.contact_rad);
     in.normal_stiffness = s->normal_stiffness[k];
     in.friction_coefficient = s->friction_coefficient[k];
     in.damping_ratio = s->damping_ratio[k];

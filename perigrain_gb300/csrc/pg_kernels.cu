@@ -269,6 +269,9 @@ __global__ void __launch_bounds__(128) k_force(const Dev P) {
       for (int c = 0; c < D; ++c) dir[c] = xq[c] - xpc[c];
       double n2 = dir[0] * dir[0];
       for (int c = 1; c < D; ++c) n2 = n2 + dir[c] * dir[c];
+      // dn <= R_c <= contact_rad needs n2 <= contact_s_max (the same outcome as the sqrt test):
+      // candidates beyond it skip the square root and the bonded-neighbour scan
+      if (!(n2 <= in.contact_s_max)) continue;
       const double dn = ieee64::sqrt_rn(n2);
       double Rc = in.contact_rad, Kn = in.normal_stiffness;
       double zeta = in.damping_ratio, mu = in.friction_coefficient;

@@ -535,6 +535,9 @@ __global__ void __launch_bounds__(128) k_force_mx(const Dev P) {
       for (int c = 0; c < D; ++c) dir64[c] = xq64[c] - xp64[c];
       double n2 = dir64[0] * dir64[0];
       for (int c = 1; c < D; ++c) n2 = n2 + dir64[c] * dir64[c];
+      // dn64 <= R_c' <= contact_rad needs n2 <= contact_s_max (the same outcome as the sqrt
+      // test): candidates beyond it skip the square root and the bonded-neighbour scan
+      if (!(n2 <= in.contact_s_max)) continue;
       const double dn64 = sqrt(n2);
       double Rc64 = in.contact_rad;
       float Kn = Kn0, zeta = zeta0, mu = mu0;

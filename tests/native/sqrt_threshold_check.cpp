@@ -1,5 +1,6 @@
-// Host check of the bond builder's threshold form (perigrain_gb300/csrc/pg_bond_threshold.h):
-// s <= bond_s_max(delta) must decide exactly as sqrt(s) <= delta for deltas of every magnitude
+// Host check of the threshold form of sqrt(s) <= delta (perigrain_gb300/csrc/pg_sqrt_threshold.h,
+// used by the bond builder and the contact test): s <= sqrt_le_max(delta) must decide exactly as
+// sqrt(s) <= delta for deltas of every magnitude
 // (grid spacings and random values, zero, negative, NaN, infinite) and s at and around delta^2
 // (every double within 64 ulps), random s, and the special values a sum of squares can take
 // (+0, +inf, NaN; never a negative number). Prints "bad 0" on success.
@@ -10,7 +11,7 @@
 #include <cstring>
 #include <random>
 
-#include "pg_bond_threshold.h"
+#include "pg_sqrt_threshold.h"
 
 static uint64_t checked = 0, bad = 0;
 static double from_bits(uint64_t b) { double x; std::memcpy(&x, &b, 8); return x; }
@@ -23,7 +24,7 @@ static void check(double delta, double smax, double s) {
 }
 
 static void around(double delta) {
-  const double smax = pg::bond_s_max(delta);
+  const double smax = pg::sqrt_le_max(delta);
   // s is a sum of squares: +0 or more, +inf or NaN, never negative
   const double specials[] = {0.0, INFINITY, NAN, 5e-324, DBL_MAX};
   for (double s : specials) check(delta, smax, s);
@@ -48,7 +49,7 @@ int main(int argc, char** argv) {
     // random deltas over the whole exponent range
     const double d = from_bits((rng() & 0x7fefffffffffffffull) | 0x0010000000000000ull);
     around(d);
-    const double smax = pg::bond_s_max(m * h);
+    const double smax = pg::sqrt_le_max(m * h);
     for (int k = 0; k < 4; ++k) check(m * h, smax, (m * h) * (m * h) * (0.5 + u(rng)));
   }
   std::printf("checked %" PRIu64 " bad %" PRIu64 "\n", checked, bad);
