@@ -145,7 +145,11 @@ typedef enum pg_node_order {
   PG_ORDER_CELL_DEGREE = 2, /* the cell order's choice, then a stable sort by bond count (most
                            bonds first), so warp chunks of the bond slab hold nodes of equal degree
                            (less padding, less coalesced neighbour gathers: the autotuner decides) */
-  PG_ORDER_SHUFFLE = 3  /* a seeded random order (tests of the order independence) */
+  PG_ORDER_SHUFFLE = 3, /* a seeded random order (tests of the order independence) */
+  PG_ORDER_CELL_BLOCK_DEGREE = 4 /* the cell order's choice, then a stable sort by bond count (most
+                           bonds first) inside consecutive windows of 256 nodes of each grain: warp
+                           chunks of nearly equal degree while every node stays within 256 places
+                           of its cell-order position (the autotuner decides) */
 } pg_node_order;
 
 /* ---- lifecycle ---------------------------------------------------------------------------- */

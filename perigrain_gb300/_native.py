@@ -48,7 +48,7 @@ class Config(C.Structure):
     ]
 
 
-NODE_ORDER = {"input": 0, "cell": 1, "cell_degree": 2, "shuffle": 3}
+NODE_ORDER = {"input": 0, "cell": 1, "cell_degree": 2, "shuffle": 3, "cell_block_degree": 4}
 
 CONF_FIELDS = [
     ("timesteps", C.c_uint32), ("modulo", C.c_uint32), ("dt", C.c_double),

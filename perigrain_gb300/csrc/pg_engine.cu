@@ -361,10 +361,12 @@ int pg_create(const pg_setup_desc* s, const pg_config* cfg_in, pg_handle** out) 
     }
   }
   // third stage: the node layout inside the grains, cell order or cell order grouped by bond count
-  // (fewer padded slots in the bond slab, less coalesced neighbour gathers)
+  // over the whole grain or inside 256-node windows (fewer padded slots in the bond slab, less
+  // coalesced neighbour gathers)
   int32_t best_order = cfg_in->node_order;
-  if (cfg_in->node_order == PG_ORDER_CELL || cfg_in->node_order == PG_ORDER_CELL_DEGREE) {
-    const int32_t orders[] = {PG_ORDER_CELL, PG_ORDER_CELL_DEGREE};
+  if (cfg_in->node_order == PG_ORDER_CELL || cfg_in->node_order == PG_ORDER_CELL_DEGREE ||
+      cfg_in->node_order == PG_ORDER_CELL_BLOCK_DEGREE) {
+    const int32_t orders[] = {PG_ORDER_CELL, PG_ORDER_CELL_DEGREE, PG_ORDER_CELL_BLOCK_DEGREE};
     double best_order_ms = 1e300;
     for (int32_t od : orders) {
       pg_config c = *cfg_in;

@@ -1,5 +1,5 @@
-// Node layout inside each grain: cell-sorted, cell-sorted then grouped by bond count, or a seeded
-// shuffle; see pg_order.h.
+// Node layout inside each grain: cell-sorted, cell-sorted then grouped by bond count (whole grain
+// or 256-node windows), or a seeded shuffle; see pg_order.h.
 #include "pg_order.h"
 
 #include <algorithm>
@@ -13,6 +13,10 @@ namespace {
 // the input's order is kept unless its mean bond index span exceeds this multiple of the cell
 // order's (measured: generated row-major meshes 1.00, the same meshes shuffled 4-9)
 constexpr double CELL_SPAN_RATIO = 1.5;
+// window of PG_ORDER_CELL_BLOCK_DEGREE: sorting by degree inside 256 consecutive nodes lifts the
+// bond slab's slot use (bonds / padded slots of 32-node chunks) from 0.80 to 0.95 on the 3D sphere
+// and settling meshes while keeping nodes near their cell-order neighbours
+constexpr uint32_t DEGREE_WINDOW = 256;
 
 uint64_t mix64(uint64_t x) {
   x += 0x9e3779b97f4a7c15ull;
@@ -79,6 +83,18 @@ bool grain_order(const pg_setup_desc* s, uint32_t n0, uint32_t n1, int32_t order
       moved = false;
     }
   }
+  auto deg_of = [&](uint32_t k) { return s->bond_offset[n0 + k + 1] - s->bond_offset[n0 + k]; };
+  if (order == PG_ORDER_CELL_BLOCK_DEGREE) {
+    // stable sort by bond count, most bonds first, inside each window of DEGREE_WINDOW nodes
+    for (uint32_t w0 = 0; w0 < n; w0 += DEGREE_WINDOW) {
+      const uint32_t w1 = std::min(n, w0 + DEGREE_WINDOW);
+      std::stable_sort(loc->begin() + w0, loc->begin() + w1,
+                       [&](uint32_t a, uint32_t b) { return deg_of(a) > deg_of(b); });
+    }
+    moved = false;
+    for (uint32_t k = 0; k < n && !moved; ++k) moved = (*loc)[k] != k;
+    return moved;
+  }
   if (order == PG_ORDER_CELL_DEGREE) {
     // stable counting sort by bond count, most bonds first
     uint64_t dmax = 0;
@@ -105,7 +121,8 @@ int make_node_order(const pg_setup_desc* s, int32_t order, NodeOrder* o, std::st
   o->bdry_nodes.clear();
   o->clamped_nodes.clear();
   if (order == PG_ORDER_INPUT) return PG_OK;
-  if (order != PG_ORDER_CELL && order != PG_ORDER_CELL_DEGREE && order != PG_ORDER_SHUFFLE) {
+  if (order != PG_ORDER_CELL && order != PG_ORDER_CELL_DEGREE && order != PG_ORDER_SHUFFLE &&
+      order != PG_ORDER_CELL_BLOCK_DEGREE) {
     *err = "unknown node_order " + std::to_string(order);
     return PG_EINVAL;
   }

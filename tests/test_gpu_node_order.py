@@ -1,8 +1,8 @@
 """The node layout inside the grains (pg_config.node_order) changes where nodes sit on the device,
 never a result: every output -- fields, the alive-bond set and break steps in CSR order, the
 contact-pair log, wall reactions, snapshots, post-processing, gradients -- is bit-identical between
-the input's order, a seeded shuffle (every node moved) and the cell order grouped by bond count,
-in FP64 and mixed precision. The reference's own orders are kept through the input indices: bond
+the input's order, a seeded shuffle (every node moved) and the cell order grouped by bond count
+(whole grain and 256-node windows), in FP64 and mixed precision. The reference's own orders are kept through the input indices: bond
 rows in NbdArr order, contact candidates in the reference's visit order, wall reactions replayed in
 node order, sums over a grain in node order. A shuffled layout is also bit-exact against the oracle."""
 import numpy as np
@@ -13,7 +13,7 @@ from perigrain_gb300 import Simulation, grad, setups
 
 pytestmark = pytest.mark.gpu
 
-ORDERS = ("input", "shuffle", "cell_degree")
+ORDERS = ("input", "shuffle", "cell_degree", "cell_block_degree")
 FIELDS = ("CurrPos", "vel", "acc", "force", "disp")
 
 
