@@ -381,5 +381,14 @@ PG_HD double widen_f32(float x) {
   return from_bits(sign | ((uint64_t)(ef + 896u) << 52) | ((uint64_t)(u & 0x7fffffu) << 29));
 }
 
+// a > b for a threshold b that is +0 or more and not NaN (gt_nonneg_ok(b)), on the integer pipe:
+// the bits of such numbers order as the numbers do, a NaN or negative a has bits above those of
+// +inf, and a = -0 or +0 is not above any such b.
+PG_HD bool gt_nonneg_ok(uint64_t b_bits) { return b_bits <= 0x7ff0000000000000ull; }
+PG_HD bool gt_nonneg(double a, uint64_t b_bits) {
+  const uint64_t ab = bits(a);
+  return ab > b_bits && ab <= 0x7ff0000000000000ull;
+}
+
 }  // namespace ieee64
 }  // namespace pg

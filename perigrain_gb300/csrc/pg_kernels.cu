@@ -150,6 +150,9 @@ __global__ void __launch_bounds__(128) k_force(const Dev P) {
   const uint32_t slot0 = P.chunk_slot[chunk] + lane;
   const uint32_t w0 = P.chunk_word[chunk];
   {
+    // the break test str > snot on the integer pipe when snot is +0 or more and not NaN
+    const uint64_t snot_bits = ieee64::bits(gr.snot);
+    const bool snot_int = ieee64::gt_nonneg_ok(snot_bits);
     double dp[D], xp[D];
     if (mov) {
       ldv<D>(P.disp, d, dp);
@@ -180,7 +183,7 @@ __global__ void __launch_bounds__(128) k_force(const Dev P) {
           const ieee64::Divisor den = ieee64::make_divisor(en);
           for (int c = 0; c < D; ++c) f[c] = f[c] + sc * ieee64::div_rn(e[c], den);
         }
-        if (brk && str > gr.snot) {
+        if (brk && (snot_int ? ieee64::gt_nonneg(str, snot_bits) : str > gr.snot)) {
           bit = false;
           P.break_step[s] = t;
         }

@@ -1,7 +1,8 @@
 // Host check of the integer FP64 division, square root, addition, subtraction, multiplication and
 // FP32 -> FP64 conversion (perigrain_gb300/csrc/pg_ieee64.cuh): their bits must equal the host's
-// IEEE `a / b`, `sqrt(x)`, `a + b`, `a - b`, `a * b` and `(double)f` on random operands of every
-// exponent (including zeros, subnormals, infinities and NaNs, which take the hardware route),
+// IEEE `a / b`, `sqrt(x)`, `a + b`, `a - b`, `a * b`, `(double)f` and `a > b` (b >= +0) on random
+// operands of every exponent (including zeros, subnormals, infinities and NaNs, which take the
+// hardware route),
 // significands at the edges of the reciprocal estimate's range, quotients near 1 and near the
 // overflow and underflow thresholds, exact squares and their neighbours, and divisors shared
 // across several quotients. Usage: ieee64_check [cases] [seed]. Prints "bad 0" on success.
@@ -43,6 +44,12 @@ static void check_widen(float x) {
   const double w = (double)x, g = pg::ieee64::widen_f32(x);
   if (!same(w, g) && (++bad_arith, bad++ < 10)) std::printf("widen %a: want %a got %a\n", (double)x, w, g);
 }
+static void check_gt(double a, double b) {
+  if (!pg::ieee64::gt_nonneg_ok(bits(b))) return;
+  ++checked;
+  if ((a > b) != pg::ieee64::gt_nonneg(a, bits(b)) && (++bad_arith, bad++ < 10))
+    std::printf("%a > %a: want %d\n", a, b, (int)(a > b));
+}
 static void check_sqrt(double x) {
   ++checked;
   const double want = std::sqrt(x), got = pg::ieee64::sqrt_rn(x);
@@ -72,6 +79,7 @@ int main(int argc, char** argv) {
     for (double b : specials) {
       check_div(a, b);
       check_arith(a, b);
+      check_gt(a, b);
     }
   }
   for (uint64_t fa : edge_frac)
@@ -100,6 +108,9 @@ int main(int argc, char** argv) {
     // products near the overflow and underflow thresholds
     check_arith(a, b);
     check_arith(c, d);
+    check_gt(a, std::fabs(b));
+    check_gt(c, std::fabs(d));
+    check_gt(from_bits(bits(std::fabs(b)) + (rng() % 5) - 2), std::fabs(b));
     {
       const double x = make(rng() & 1, 1023 - 30 + rng() % 60, frac());
       const int de = (int)(rng() % 130) - 65;
