@@ -333,9 +333,10 @@ __global__ void __launch_bounds__(32 * SUB) k_adj_bonds(const Dev P, const AdjSt
 // warp w takes the node's contact entries i = w, w+SUB, ..., warp 0 also the walls; the partial
 // cotangents are summed in shared memory in a fixed order and warp 0 adds the bond share from
 // k_adj_bonds and runs the integrator. For the FP32 bond path it also writes the force cotangent
-// of the next reverse step to fbf.
+// of the next reverse step to fbf. In 2D at most 128 registers, 4 blocks per SM (138 unbounded,
+// 3 per SM: a 592-chunk handle then ran 1.3 waves); 3D keeps its 168 registers, 3 blocks per SM.
 template <int D>
-__global__ void __launch_bounds__(32 * SUB) k_adj_rest(const Dev P, const AdjStep A) {
+__global__ void __launch_bounds__(32 * SUB, D == 2 ? 4 : 3) k_adj_rest(const Dev P, const AdjStep A) {
   pdl_enter();
   constexpr int NS = 2 * D;
   constexpr int NV = 2 * D + NPARAM;  // xb[D], vfb[D], pc[NPARAM]
