@@ -1,6 +1,7 @@
-"""The integer FP64 division and square root of the FP64 force kernel (pg_ieee64.cuh) give the
-bits of IEEE `a / b` and `sqrt(x)`: host build of the same routines (tests/native/ieee64_check.cpp)
-against the host's IEEE operations, with the FP32 estimates exact and with them scaled by
+"""The integer FP64 routines of the kernels (pg_ieee64.cuh: division, square root, addition,
+subtraction, multiplication, FP32 -> FP64 conversion, the compare a > b for b >= +0) give the bits
+of the IEEE operations: host build of the same routines (tests/native/ieee64_check.cpp) against the
+host's IEEE operations, with the FP32 estimates exact and with them scaled by
 1 +- 2^-20, at least four times the error of the GPU's estimates, to check the correction margins.
 CPU only."""
 import os
