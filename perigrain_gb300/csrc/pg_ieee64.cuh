@@ -33,9 +33,9 @@
 // Addition, subtraction and multiplication (add_rn, sub_rn, mul_rn) and the FP32 -> FP64
 // conversion (widen_f32) are provided the same way. Measured in the FP64 force kernel's bond loop
 // (bond vector e = (dj - dp) + (xj - xp)) and in the mixed path's position update, the integer
-// sum was slower than the FP64 instruction it replaced (about 40 integer instructions against one
-// FP64 add), so the kernels use only the division and square root; the others are kept, with
-// their checks, for loops where the FP64 pipe is busier.
+// sum was slower than the FP64 instruction it replaced (about 40 integer instructions with
+// branches against one FP64 add); the nearly branch-free product pays off for the squares of the
+// bond length, which is where the FP64 force kernel uses it.
 //
 // Host and device share the code, so the routines are tested bit for bit against the host's
 // IEEE operations as well as against the GPU's.

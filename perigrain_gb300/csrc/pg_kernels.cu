@@ -170,8 +170,10 @@ __global__ void __launch_bounds__(128) k_force(const Dev P) {
         ldv<D>(P.xpos, j, xj);
         double e[D];
         for (int c = 0; c < D; ++c) e[c] = (dj[c] - dp[c]) + (xj[c] - xp[c]);
-        double n2 = e[0] * e[0];
-        for (int c = 1; c < D; ++c) n2 = n2 + e[c] * e[c];
+        // the squares on the integer pipe too (the sums stay FP64 instructions: the integer sum
+        // measured slower, and so did moving the scale and force products as well)
+        double n2 = ieee64::mul_rn(e[0], e[0]);
+        for (int c = 1; c < D; ++c) n2 = n2 + ieee64::mul_rn(e[c], e[c]);
         // sqrt and the divisions on the integer pipe, bit-identical to the IEEE operations
         const double en = ieee64::sqrt_rn(n2);
         const double str = ieee64::div_rn(en - xin, xin);
