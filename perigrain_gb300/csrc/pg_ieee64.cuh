@@ -1,4 +1,7 @@
-// Correctly rounded FP64 division and square root computed on the integer and FP32 pipes.
+// Correctly rounded FP64 arithmetic computed on the integer and FP32 pipes: division and square
+// root (used by the FP64 force kernel and the packing ascent), multiplication (the FP64 force
+// kernel's squared bond length), addition, subtraction, FP32 -> FP64 conversion and an ordered
+// compare against a non-negative threshold.
 //
 // GB300 executes FP64 arithmetic at about 1/64 of its FP32 rate, and an IEEE FP64 division or
 // square root expands to about ten FP64 instructions, while the integer and FP32 pipes are some
