@@ -264,6 +264,11 @@ int pg_get_contact_skin(pg_handle* h, double* skin);
 /* Node layout in use: the pg_node_order asked for (after autotuning), and whether it differs from
  * the input's order (0: the input already was in that order, or PG_ORDER_INPUT). */
 int pg_get_node_order(pg_handle* h, int32_t* order, int32_t* permuted);
+/* Test hook of the node layout, on the host only (no device needed): validates the setup as
+ * pg_create does without a device (bond rows included) and fills perm[i] = the input index of
+ * device node i (n_nodes entries) for the pg_node_order `order`, and *permuted = 0 when that is the
+ * input order itself. */
+int pg_debug_node_order(const pg_setup_desc* s, int32_t order, uint32_t* perm, int32_t* permuted);
 /* Number of kernel launches issued by the last pg_step call. */
 int pg_get_launch_count(pg_handle* h, uint64_t* launches);
 /* Per-kernel device time of the last pg_step call (CUDA events; needs timing enabled). */

@@ -127,6 +127,7 @@ PROTOTYPES = [
     ("pg_get_launch_config", C.c_int, [C.c_void_p, u32p, u32p]),
     ("pg_get_contact_skin", C.c_int, [C.c_void_p, f64p]),
     ("pg_get_node_order", C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    ("pg_debug_node_order", C.c_int, [C.POINTER(SetupDesc), C.c_int32, C.c_void_p, C.POINTER(C.c_int32)]),
     ("pg_set_timing", C.c_int, [C.c_void_p, C.c_int32]),
     ("pg_get_kernel_times", C.c_int, [C.c_void_p, f64p, f64p, u64p]),
     ("pg_build_bonds", C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_double, C.c_void_p, C.c_uint64, u64p,

@@ -1302,6 +1302,21 @@ int pg_get_node_order(pg_handle* h, int32_t* order, int32_t* permuted) {
   return PG_OK;
 }
 
+int pg_debug_node_order(const pg_setup_desc* s, int32_t order, uint32_t* perm, int32_t* permuted) {
+  pg_config c;
+  pg_config_default(&c);
+  int rc = validate(s, &c, true);
+  if (rc) return rc;
+  if (!perm) return fail(PG_EINVAL, "null perm");
+  NodeOrder ord;
+  std::string err;
+  rc = make_node_order(s, order, &ord, &err);
+  if (rc) return fail(rc, err);
+  for (uint32_t i = 0; i < s->n_nodes; ++i) perm[i] = ord.perm.empty() ? i : ord.perm[i];
+  if (permuted) *permuted = ord.perm.empty() ? 0 : 1;
+  return PG_OK;
+}
+
 int pg_get_contact_skin(pg_handle* h, double* skin) {
   if (!h || !skin) return fail(PG_EINVAL, "null argument");
   *skin = h->contact_skin;
